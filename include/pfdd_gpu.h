@@ -1,0 +1,155 @@
+/*
+ * pfdd_gpu.h -- C ABI of the GB300-native PFDD TDGL hot path.
+ *
+ * The reference program (trungnnguyen/PFDD2, one C file PFDD_Final_GPU.c,
+ * cited F:<line>) runs its TDGL loop in `main` (F:4574-4691): copy xi to a
+ * float buffer, `fft_forward(data, NSV)`, contract with the interaction matrix
+ * B(k), `fft_backward(data2, NS)`, then `plasticevolv` (F:3470-3501).  Its
+ * swappable boundary is the FFT pair `fft_forward(float*, int batch)` /
+ * `fft_backward(float*, int batch)` (F:209-273) with FOURN, FFTW or cuFFT
+ * behind it.  This library replaces both levels:
+ *
+ *   - the whole step (pfdd_create .. pfdd_step .. pfdd_get_state), with xi,
+ *     B(k) and the spectral work buffers resident on the GPU, and
+ *   - the FFT boundary itself (pfdd_fft_*), a drop-in for fft_forward /
+ *     fft_backward on caller-owned host or device buffers.
+ *
+ * Conventions (all from the reference):
+ *   - grid N1 x N2 x N3, each a power of two in [1, 512]; N = N1*N2*N3;
+ *   - field layout [field][i][j][k] with k fastest, complex values
+ *     interleaved [re, im] (F:38-65);
+ *   - forward transform exp(-2 pi i n.k / N), backward exp(+2 pi i n.k / N),
+ *     neither normalised (F:209-273); the step divides by N as
+ *     plasticevolv does (F:3488-3489);
+ *   - the constant pi in the update is the reference's truncated
+ *     3.141592654 (F:95).
+ *
+ * Every call returns a status; nothing calls exit() or assert().  A context
+ * is used by one host thread at a time; distinct contexts may be driven from
+ * distinct threads (each owns its own CUDA stream).
+ */
+#ifndef PFDD_GPU_H
+#define PFDD_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PFDD_OK = 0,
+  PFDD_EINVAL = 1,      /* bad argument (size, pointer, replica index, state) */
+  PFDD_ENOMEM = 2,      /* device or host allocation failed */
+  PFDD_ECUDA = 3,       /* a CUDA runtime call failed; see pfdd_last_error */
+  PFDD_ETIMEOUT = 4,    /* a bounded device-side wait ran out */
+  PFDD_ENONFINITE = 5,  /* the state became NaN/Inf (divergence watchdog) */
+  PFDD_ENOTREADY = 6    /* a required input (B, parameters, state) was not set */
+} pfdd_status;
+
+typedef enum {
+  PFDD_FP64 = 0,      /* plain form: FFTs, contraction and update in FP64 */
+  PFDD_FFT_FP32 = 1   /* precision form: complex64 FFTs + FP32 contraction, FP64 state/sums */
+} pfdd_precision;
+
+typedef struct pfdd_ctx pfdd_ctx;
+
+/* ---- whole-step interface: replaces F:4574-4691 -------------------------- */
+
+/* One solve.  Replaces the allocations of F:4137-4166 for the hot path. */
+pfdd_status pfdd_create(pfdd_ctx **ctx, int n1, int n2, int n3, int ns, int precision, int device);
+
+/* `nrep` independent solves of the same grid/system count that share one B(k)
+ * (batched replicas / serving slots).  nrep >= 1. */
+pfdd_status pfdd_create_batched(pfdd_ctx **ctx, int n1, int n2, int n3, int ns, int nrep, int precision,
+                                int device);
+
+void pfdd_destroy(pfdd_ctx *ctx);
+
+/* Message of the last failed call on this context ("" if none). */
+const char *pfdd_last_error(const pfdd_ctx *ctx);
+
+/* Interaction matrix from host memory, FP64, the reference's BB layout
+ * restricted to the slip block: B[kb][ka][i][j][k] for ka, kb < ns
+ * (F:59 with I5, filled by Bmatrix F:328-412).  Copied; symmetric in (ka,kb). */
+pfdd_status pfdd_set_B(pfdd_ctx *ctx, const double *B);
+
+/* Builds B(k) on the device in FP64 from the cubic elastic constants and the
+ * eigenstrains eps[ns][3][3] (seteps F:1912-1980), grid spacings d1,d2,d3 and
+ * the frequency convention of frec (F:2683-2754).  Same formula as Bmatrix
+ * (F:328-412), evaluated in closed form.  FP32 contexts round it after. */
+pfdd_status pfdd_build_B(pfdd_ctx *ctx, double C11, double C12, double C44, const double *eps, double d1,
+                         double d2, double d3);
+
+/* Copies the context's B(k) back to the host as FP64 in the pfdd_set_B layout
+ * B[kb][ka][N] (FP32 contexts return their rounded values).  Replaces reading
+ * the reference's BB array after Bmatrix (F:4325). */
+pfdd_status pfdd_get_B(pfdd_ctx *ctx, double *B);
+
+/* Kinetic and core-energy coefficients per slip system (CD2, Asf2, dslip2 of
+ * F:4277-4297, 2495-2498) and the scalar uq2 (F:4194). */
+pfdd_status pfdd_set_params(pfdd_ctx *ctx, const double *cd2, const double *asf, const double *dslip, double uq2);
+
+/* Order parameter and boundary flags of every replica:
+ * xi[nrep][ns][N][2] and xi_bc[nrep][ns][N][2] (xi.dat / xi_bc.dat layout for
+ * the slip fields, F:4366-4382).  A point evolves where xi_bc[...][0] == 0
+ * (F:3481).  xi_bc may be NULL: every point evolves. */
+pfdd_status pfdd_set_state(pfdd_ctx *ctx, const double *xi, const double *xi_bc);
+
+/* Same for one replica r (xi[ns][N][2]); the other replicas are untouched. */
+pfdd_status pfdd_set_replica_state(pfdd_ctx *ctx, int r, const double *xi, const double *xi_bc);
+
+/* Optional spatially varying resolved shear stress tau(x) (resolSS,
+ * F:1540-1637), layout tau_field[i][j][k][ns] like the reference's tau array;
+ * shared by all replicas.  When set, the per-step values passed to pfdd_step
+ * multiply it (the stress-ramp factor); NULL clears it. */
+pfdd_status pfdd_set_tau_field(pfdd_ctx *ctx, const double *tau_field);
+
+/* Runs `nsteps` explicit Euler TDGL steps (plasticevolv, F:3470-3501; loop
+ * F:4574-4691).  tau[nsteps][nrep][ns] is the resolved shear stress of each
+ * step (or the multiplier of the tau field).  Outputs, if non-NULL:
+ * gamma[nsteps][nrep] (average plastic strain, F:3494) and
+ * gamma_a[nsteps][nrep][ns] (per system, F:3495). */
+pfdd_status pfdd_step(pfdd_ctx *ctx, int nsteps, const double *tau, double *gamma, double *gamma_a);
+
+/* Copies xi of every replica back: xi[nrep][ns][N][2]. */
+pfdd_status pfdd_get_state(pfdd_ctx *ctx, double *xi);
+pfdd_status pfdd_get_replica_state(pfdd_ctx *ctx, int r, double *xi);
+
+/* Marks replica r active (1) or idle (0).  Idle replicas are skipped by every
+ * kernel of a step and keep their state (serving slots). */
+pfdd_status pfdd_set_replica_active(pfdd_ctx *ctx, int r, int active);
+
+/* Number of kernel launches issued by the last pfdd_step call. */
+long long pfdd_last_launch_count(const pfdd_ctx *ctx);
+
+/* Device bytes held by a context of this shape (admission control). */
+size_t pfdd_required_bytes(int n1, int n2, int n3, int ns, int nrep, int precision);
+
+/* ---- FFT boundary: drop-in for fft_forward / fft_backward (F:209-273) ---- */
+
+typedef struct pfdd_fft_plan pfdd_fft_plan;
+
+/* Plan for in-place, unnormalised 3D C2C transforms of an N1 x N2 x N3 grid
+ * (cufftPlan3d(N1,N2,N3,CUFFT_C2C) of F:170-173).  precision selects complex64
+ * (PFDD_FFT_FP32, the reference's float buffers) or complex128 (PFDD_FP64,
+ * the -Dfloat=double build).  max_batch bounds `batch` below. */
+pfdd_status pfdd_fft_plan_create(pfdd_fft_plan **plan, int n1, int n2, int n3, int precision, int max_batch,
+                                 int device);
+void pfdd_fft_plan_destroy(pfdd_fft_plan *plan);
+
+/* fft_forward(data, batch) / fft_backward(data, batch): `batch` contiguous
+ * fields of 2*N values each, interleaved complex.  `data` is a host pointer
+ * (copied to the device and back, as the reference's `acc data copy` does,
+ * F:4446-4450) or a device pointer (on_device = 1).  float for FP32 plans,
+ * double for FP64 plans. */
+pfdd_status pfdd_fft_forward(pfdd_fft_plan *plan, void *data, int batch, int on_device);
+pfdd_status pfdd_fft_backward(pfdd_fft_plan *plan, void *data, int batch, int on_device);
+
+const char *pfdd_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFDD_GPU_H */

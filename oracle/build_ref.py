@@ -1,0 +1,221 @@
+"""Build recipe for the patched reference program (test infrastructure only).
+
+The reference is one C program, ``PFDD_Final_GPU.c``.  As shipped it never runs
+a TDGL step (``NTD=0``), pins every slip system and has a refactoring
+regression in ``virtualevolv``; to use it as an oracle for the TDGL hot path we
+apply a small, line-anchored patch set to a build-time copy and compile that
+copy with gcc.  Every patch is verified against the original line text, so a
+different reference revision fails loudly instead of building something else.
+
+The patched source and the binaries go to ``oracle/_ref/`` only (git-ignored).
+On a machine without the reference checkout (the GPU host) the previously
+generated ``oracle/_ref/pfdd_ref_patched.c`` is recompiled for the local
+architecture, which is why that generated file is kept beside the binaries.
+
+Patch set (line numbers of ``PFDD_Final_GPU.c``):
+
+==  =========================  ====================================================
+#   where                      what
+==  =========================  ====================================================
+1   82-86, 91                  NMAT=1, grid from -D, NS1=12 (FCC), NTD=2 (one
+                               outer step runs the inner TDGL loop)
+2   4315, 1903                 ``setfcc`` instead of ``set3D1sys``; Burgers vector
+                               scaled by ``PFDD_BDIV`` (sqrt(2) gives |b|=1)
+3   4186                       ``choice=2``: read xi.dat / xi_bc.dat
+4   4205                       ``plastic_max = PFDD_K`` (fixed step count)
+5   4580                       ``interfacevolv`` disabled (bimaterial special case)
+6   1432                       regression fix: the virtual DD term is not added to
+                               slip row ``isb`` (the older program's semantics)
+7   302-304, 4278-4281, 4297   mu = C44, lambda = C12, Asf2 and CD2 from -D
+8   3876-3877, 3484, 3488      applied sigma_xz = PFDD_SIGMA, ramped by
+                               (it_plastic+1)/K inside ``plasticevolv``
+9   4442-4532, 4616-4645,      diagnostics that never feed xi (energies, strain,
+    4326, 4329                 gradient term) behind ``PFDD_DIAG``
+10  4325, 4157-4162            ``Bmatrix`` behind ``PFDD_SETUP_B`` (timing builds
+                               only); big tables calloc'ed
+11  4672                       extra full-precision per-step log (gamma_full.dat):
+                               step, gamma, gamma_a[0..NS-1], wall-clock time
+==  =========================  ====================================================
+"""
+from __future__ import annotations
+
+import os
+import platform
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_DIR = HERE / "_ref"
+REF_SRC = Path("/root/reference/PFDD_Final_GPU.c")
+PATCHED = REF_DIR / "pfdd_ref_patched.c"
+
+DEFAULTS_BLOCK = r"""
+/* ---- defaults for the build-time patch set (values come from -D) ---- */
+#ifndef PFDD_N1
+#define PFDD_N1 32
+#endif
+#ifndef PFDD_N2
+#define PFDD_N2 32
+#endif
+#ifndef PFDD_N3
+#define PFDD_N3 32
+#endif
+#ifndef PFDD_K
+#define PFDD_K 20
+#endif
+#ifndef PFDD_SIGMA
+#define PFDD_SIGMA 0.0
+#endif
+#ifndef PFDD_MU
+#define PFDD_MU 1.0
+#endif
+#ifndef PFDD_LAMBDA
+#define PFDD_LAMBDA 1.5
+#endif
+#ifndef PFDD_ASF
+#define PFDD_ASF 0.1
+#endif
+#ifndef PFDD_CD2
+#define PFDD_CD2 0.01
+#endif
+#ifndef PFDD_BDIV
+#define PFDD_BDIV sqrt(2.0)
+#endif
+#ifndef PFDD_DIAG
+#define PFDD_DIAG 1
+#endif
+#ifndef PFDD_SETUP_B
+#define PFDD_SETUP_B 1
+#endif
+#define PFDD_LOG_STEP(itp_, g_, g1_) do { static FILE *pfdd_gf_; int q_; \
+    if (!pfdd_gf_) pfdd_gf_ = fopen("gamma_full.dat", "w"); \
+    fprintf(pfdd_gf_, "%d %.17e", (itp_), (double)(g_)); \
+    for (q_ = 0; q_ < NS; q_++) fprintf(pfdd_gf_, " %.17e", (double)(g1_)[q_]); \
+    fprintf(pfdd_gf_, " %.9f\n", WTime()); fflush(pfdd_gf_); } while (0)
+"""
+
+# (1-based line, original substring, replacement substring)
+PATCHES = [
+    (26, "#include <sys/time.h>", "#include <sys/time.h>\n" + DEFAULTS_BLOCK),
+    (82, "#define NMAT 2", "#define NMAT 1"),
+    (83, "#define N1 32", "#define N1 PFDD_N1"),
+    (84, "#define N2 2 ", "#define N2 PFDD_N2 "),
+    (85, "#define N3 32", "#define N3 PFDD_N3"),
+    (86, "#define NS1 1 ", "#define NS1 12 "),
+    (91, "#define NTD 0/", "#define NTD 2/"),
+    (302, "mc->C11=168.4E9;", "mc->C11=2.0*PFDD_MU+PFDD_LAMBDA;"),
+    (303, "mc->C12=121.4E9;", "mc->C12=PFDD_LAMBDA;"),
+    (304, "mc->C44=23.5E9;", "mc->C44=PFDD_MU;"),
+    (1432, "if(isa >= NS) {", "if(0) {"),
+    (1903, "xb[i][j] = xb[i][j]/2.0;", "xb[i][j] = xb[i][j]/PFDD_BDIV;"),
+    (3484, "-tau[i][j][k][isa]/dslip2[isa]", "-tau[i][j][k][isa]*((it_plastic+1.0)/PFDD_K)/dslip2[isa]"),
+    (3488, "-tau[i][j][k][isa]/dslip2[isa]", "-tau[i][j][k][isa]*((it_plastic+1.0)/PFDD_K)/dslip2[isa]"),
+    (3876, "if ((u==0&&v==1) || (u==1&&v==0)) {", "if ((u==0&&v==2) || (u==2&&v==0)) {"),
+    (3877, "sigma[i][j][k][u][v] = 0.0;", "sigma[i][j][k][u][v] = PFDD_SIGMA;"),
+    (4157, "BB = malloc((NS)*(NSV)*(N1)*(N2)*(N3)*sizeof(double));",
+     "BB = calloc((size_t)(NS)*(NSV)*(N1)*(N2)*(N3), sizeof(double));"),
+    (4158, "FF = malloc((NS)*(N1)*(N2)*(N3)*(ND)*(ND)*sizeof(double));",
+     "FF = calloc((size_t)(NS)*(N1)*(N2)*(N3)*(ND)*(ND), sizeof(double));"),
+    (4159, "DD = malloc((NSV)*(N1)*(N2)*(N3)*(ND)*(ND)*sizeof(double));",
+     "DD = calloc((size_t)(NSV)*(N1)*(N2)*(N3)*(ND)*(ND), sizeof(double));"),
+    (4160, "FFv = malloc((NV)*(N1)*(N2)*(N3)*(ND)*(ND)*sizeof(double));",
+     "FFv = calloc((size_t)(NV)*(N1)*(N2)*(N3)*(ND)*(ND), sizeof(double));"),
+    (4162, "GG = malloc((2*(NS)*(NS)*(N1)*(N2)*(N3))*sizeof(double));",
+     "GG = calloc((size_t)(2*(NS)*(NS)*(N1)*(N2)*(N3)), sizeof(double));"),
+    (4186, "choice=1;", "choice=2;"),
+    (4205, "plastic_max =3000;", "plastic_max =PFDD_K;"),
+    (4278, "Asf2[is] = 0.0262;", "Asf2[is] = PFDD_ASF;"),
+    (4280, "Asf2[0] = 0.0064659518668288441;", "Asf2[0] = PFDD_ASF;"),
+    (4281, "Asf2[1] = 0.0064659518668288441;", "Asf2[1] = PFDD_ASF;"),
+    (4297, "CD2[is] = 0.1;", "CD2[is] = PFDD_CD2;"),
+    (4315, "set3D1sys(xn,xb);", "setfcc(xn,xb);"),
+    (4325, "Bmatrix(BB, fx,", "if (PFDD_SETUP_B) Bmatrix(BB, fx,"),
+    (4326, "Fmatrix(FF, DD,", "if (PFDD_DIAG) Fmatrix(FF, DD,"),
+    (4329, "Gmatrix (GG,", "if (PFDD_DIAG) Gmatrix (GG,"),
+    (4442, "energy_in3 = avestrain(", "energy_in3 = (!PFDD_DIAG) ? 0 : avestrain("),
+    (4443, "energy_in2 = Imatrix(", "energy_in2 = (!PFDD_DIAG) ? 0 : Imatrix("),
+    (4458, "fft_backward(datag, NS);", "if (PFDD_DIAG) fft_backward(datag, NS);"),
+    (4461, "calc_strain_stress(databeta,", "if (PFDD_DIAG) calc_strain_stress(databeta,"),
+    (4530, "energy_in = Energy_calculation(", "energy_in = (!PFDD_DIAG) ? 0 : Energy_calculation("),
+    (4532, "energy_Residual = ResidualEnergy(", "energy_Residual = (!PFDD_DIAG) ? 0 : ResidualEnergy("),
+    (4580, "interfacevolv(xi,", "if(0)interfacevolv(xi,"),
+    (4643, "fft_backward(datag, NS);", "if (PFDD_DIAG) fft_backward(datag, NS);"),
+    (4645, "if (1) {//checkpass==1", "if (PFDD_DIAG) {//checkpass==1"),
+    (4672, "gamma1[0],gamma1[1],gamma);", "gamma1[0],gamma1[1],gamma); PFDD_LOG_STEP(it_plastic, gamma, gamma1);"),
+]
+# the inner-loop gradient contraction ("if(isb<NS){" below line 4600)
+INNER_DATAG = ("if(isb<NS){", "if(PFDD_DIAG && isb<NS){", 4600, 4630)
+
+
+def write_patched_source(src: Path = REF_SRC, dst: Path = PATCHED) -> Path:
+    """Apply the patch set to the reference source and write the result to ``dst``."""
+    raw = src.read_bytes().decode("latin-1")
+    lines = raw.split("\n")  # keeps the trailing '\r' of CRLF lines
+    for ln, old, new in PATCHES:
+        text = lines[ln - 1]
+        if text.count(old) != 1:
+            raise RuntimeError(f"patch at line {ln}: expected one '{old}' in {text!r}")
+        lines[ln - 1] = text.replace(old, new)
+    old, new, lo, hi = INNER_DATAG
+    hits = [i for i in range(lo - 1, hi) if old in lines[i]]
+    if len(hits) != 1:
+        raise RuntimeError(f"inner datag patch: {len(hits)} matches")
+    lines[hits[0]] = lines[hits[0]].replace(old, new)
+    dst.parent.mkdir(parents=True, exist_ok=True)
+    dst.write_bytes("\n".join(lines).encode("latin-1"))
+    return dst
+
+
+def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01) -> str:
+    tag = "x".join(str(int(v)) for v in n)
+    return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}_{'fp64' if fp64 else 'fp32'}"
+            f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}")
+
+
+def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=True,
+                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False) -> Path:
+    """Compile one configuration of the patched reference; returns the binary path."""
+    if REF_SRC.exists() and (force or not PATCHED.exists()
+                             or PATCHED.stat().st_mtime < Path(__file__).stat().st_mtime):
+        write_patched_source()
+    if not PATCHED.exists():
+        raise FileNotFoundError("patched reference source missing (no reference checkout here)")
+    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2)
+    if out.exists() and out.stat().st_mtime >= PATCHED.stat().st_mtime and not force:
+        return out
+    defs = [f"-DPFDD_N1={n[0]}", f"-DPFDD_N2={n[1]}", f"-DPFDD_N3={n[2]}", f"-DPFDD_K={k}",
+            f"-DPFDD_SIGMA={sigma!r}", f"-DPFDD_ASF={asf!r}", f"-DPFDD_CD2={cd2!r}",
+            f"-DPFDD_MU={mu!r}", f"-DPFDD_LAMBDA={lam!r}",
+            f"-DPFDD_DIAG={1 if diag else 0}", f"-DPFDD_SETUP_B={1 if setup_b else 0}"]
+    if fp64:
+        defs.append("-Dfloat=double")
+    cmd = ["gcc", "-O2", "-w", "-DUSE_FOURN", *defs]
+    if platform.machine() == "x86_64":
+        cmd.append("-mcmodel=medium")
+    cmd += ["-o", str(out), str(PATCHED), "-lm"]
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def bench_variants():
+    """Reference builds the CPU-baseline legs time: the stock FP32 spectral build at
+    128^3 x 12 (FCC), hot path only (diagnostics off), B(k) setup skipped because
+    only the per-step time is measured (the step's work does not depend on B's
+    values), K = 1000 ramp as in the 128^3 workload."""
+    return [dict(n=(128, 128, 128), k=1000, sigma=0.05, fp64=False, diag=False, setup_b=False),
+            dict(n=(128, 128, 128), k=1000, sigma=0.05, fp64=True, diag=False, setup_b=False)]
+
+
+def run_ref(binary: Path, workdir: Path, timeout=None, quiet=True):
+    """Run a patched-reference binary in ``workdir`` (which must hold xi.dat and xi_bc.dat)."""
+    with open(workdir / "stdout.log", "w") as fo:
+        subprocess.run([str(binary)], cwd=workdir, check=True, timeout=timeout,
+                       stdout=fo if quiet else None, stderr=subprocess.STDOUT)
+
+
+if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "source":
+        print(write_patched_source())
+    else:
+        print(compile_ref(force=True))

@@ -1,0 +1,139 @@
+"""ctypes front end of the CPU FP64 oracle (oracle/pfdd_cpu.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, ``__graft_entry__.smoke()`` and bench.py's
+CPU-baseline legs to check and time the CUDA path; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "pfdd_cpu.c"
+BUILD = HERE / "_build"
+LIB = BUILD / "libpfdd_oracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the restatement (gcc -O2, no FP contraction so x86 and Arm agree bitwise)."""
+    BUILD.mkdir(exist_ok=True)
+    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp), str(SRC),
+                    "-lm", "-lpthread"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+        L.oracle_frec.argtypes = [C.c_int, C.c_double, dp]
+        L.oracle_setfcc.argtypes = [dp, dp, C.c_double, C.c_int]
+        L.oracle_setorient.argtypes = [dp]
+        L.oracle_seteps.argtypes = [C.c_int, dp, dp, dp, dp, dp]
+        L.oracle_resolss_uniform.argtypes = [C.c_int, dp, dp, dp]
+        L.oracle_bmatrix.argtypes = [C.c_int] * 3 + [C.c_double] * 6 + [C.c_int, dp, dp, C.c_int]
+        L.oracle_fft3d.argtypes = [C.c_int] * 4 + [dp, C.c_int, C.c_int]
+        L.oracle_run.argtypes = ([C.c_int] * 4 + [dp, dp, dp, dp, dp, dp, C.c_double, C.c_int, dp,
+                                 C.c_void_p, dp, dp, C.c_int])
+        L.oracle_run.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def nthreads() -> int:
+    return max(1, min(64, os.cpu_count() or 1))
+
+
+def frec(n: int, d: float = 1.0) -> np.ndarray:
+    f = np.zeros(n)
+    lib().oracle_frec(n, d, f)
+    return f
+
+
+def fcc_eps(ns: int = 12, bdiv: float = float(np.sqrt(2.0)), dslip=None, float_s3: bool = False) -> np.ndarray:
+    """Eigenstrains of the first ``ns`` FCC systems in the global frame, shape [ns, 3, 3]."""
+    xn = np.zeros((12, 3)); xb = np.zeros((12, 3)); th = np.zeros((3, 3))
+    lib().oracle_setfcc(xn, xb, bdiv, int(float_s3))
+    lib().oracle_setorient(th)
+    ds = np.ones(12) if dslip is None else np.ascontiguousarray(dslip, dtype=np.float64)
+    eps = np.zeros((12, 3, 3))
+    lib().oracle_seteps(12, xn, xb, ds, th, eps)
+    return eps[:ns].copy()
+
+
+def resolved_shear(eps: np.ndarray, sigma: np.ndarray) -> np.ndarray:
+    tau = np.zeros(eps.shape[0])
+    lib().oracle_resolss_uniform(eps.shape[0], np.ascontiguousarray(sigma, dtype=np.float64),
+                                 np.ascontiguousarray(eps), tau)
+    return tau
+
+
+def bmatrix(n, eps: np.ndarray, C11: float, C12: float, C44: float, d=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """Interaction matrix, layout [kb][ka][n1][n2][n3] like the reference's BB."""
+    ns = eps.shape[0]
+    B = np.zeros((ns, ns) + tuple(n))
+    lib().oracle_bmatrix(n[0], n[1], n[2], d[0], d[1], d[2], C11, C12, C44, ns, np.ascontiguousarray(eps), B,
+                         nthreads())
+    return B
+
+
+def fft3d(x: np.ndarray, sign: int) -> np.ndarray:
+    """Unnormalised 3D C2C transform of complex128 fields [nf, n1, n2, n3]."""
+    a = np.ascontiguousarray(np.stack([x.real, x.imag], axis=-1))
+    lib().oracle_fft3d(x.shape[1], x.shape[2], x.shape[3], x.shape[0], a, int(sign), nthreads())
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def ramp_tau(tau_max: np.ndarray, steps: int) -> np.ndarray:
+    """Per-step resolved shear stress tau_max * (s+1)/K, evaluated as the patched
+    reference does inside plasticevolv: tau * ((it_plastic + 1.0) / K)."""
+    s = np.arange(steps, dtype=np.float64)
+    return tau_max[None, :] * ((s[:, None] + 1.0) / float(steps))
+
+
+def run(n, B: np.ndarray, xi: np.ndarray, bc: np.ndarray, cd2, asf, dslip, uq2: float, tau_steps: np.ndarray,
+        tau_field: np.ndarray | None = None):
+    """Run ``len(tau_steps)`` TDGL steps; returns (xi_final, gamma[K], gamma_a[K, ns])."""
+    ns = xi.shape[0]
+    K = tau_steps.shape[0]
+    x = np.ascontiguousarray(np.stack([xi.real, xi.imag], axis=-1))
+    b = np.ascontiguousarray(np.stack([bc, bc], axis=-1).astype(np.float64))
+    g = np.zeros(K); ga = np.zeros((K, ns))
+    tf = None if tau_field is None else np.ascontiguousarray(tau_field, dtype=np.float64)
+    rc = lib().oracle_run(n[0], n[1], n[2], ns, np.ascontiguousarray(B), x, b,
+                          np.ascontiguousarray(cd2, dtype=np.float64), np.ascontiguousarray(asf, dtype=np.float64),
+                          np.ascontiguousarray(dslip, dtype=np.float64), float(uq2), K,
+                          np.ascontiguousarray(tau_steps, dtype=np.float64),
+                          None if tf is None else tf.ctypes.data_as(C.c_void_p), g, ga, nthreads())
+    if rc != 0:
+        raise MemoryError("oracle_run failed")
+    return x[..., 0] + 1j * x[..., 1], g, ga
+
+
+def solve(spec, steps: int | None = None, eps_bdiv: float = float(np.sqrt(2.0))):
+    """Full oracle solve of a :class:`pfdd_gb300.workloads.SolveSpec` (first ``steps`` steps)."""
+    from pfdd_gb300 import workloads
+    K = spec.steps if steps is None else steps
+    eps = fcc_eps(spec.ns, bdiv=eps_bdiv, dslip=np.full(12, spec.dslip))
+    C44, C12 = spec.mu, spec.lam
+    C11 = 2.0 * C44 + C12
+    B = bmatrix(spec.n, eps, C11, C12, C44, spec.d)
+    sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
+    tau_max = resolved_shear(eps, sig)
+    tau = ramp_tau(tau_max, spec.steps)[:K]
+    xi, bc = workloads.initial_state(spec)
+    ns = spec.ns
+    return run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf), np.full(ns, spec.dslip), 1.0, tau)

@@ -1,0 +1,85 @@
+"""In-tree build of the native library and the C host driver (nvcc/gcc, no cmake).
+
+Outputs (git-ignored): ``pfdd_gb300/_lib/libpfdd_gb300.so`` and
+``pfdd_gb300/_lib/pfdd_run`` (the C host driver, linked against the library).
+All CUDA code is compiled for sm_103a only.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+HOST = PKG / "host"
+LIBDIR = PKG / "_lib"
+LIB = LIBDIR / "libpfdd_gb300.so"
+RUNNER = LIBDIR / "pfdd_run"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
+
+CU_SOURCES = ["pfdd_api.cu"]
+C_SOURCES = ["pfdd_setup.c"]
+
+
+def _nvcc() -> str:
+    cand = os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/bin/nvcc"
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def _deps() -> list[Path]:
+    return (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.c")) + list(CSRC.glob("*.h"))
+            + list((ROOT / "include").glob("*.h")) + list(HOST.glob("*.c")) + [Path(__file__)])
+
+
+def _stale(target: Path) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in _deps())
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile every translation unit in parallel and link the shared library."""
+    LIBDIR.mkdir(exist_ok=True)
+    if not force and not _stale(LIB) and not _stale(RUNNER):
+        return LIB
+    objdir = LIBDIR / "obj"
+    objdir.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    for src in CU_SOURCES:
+        obj = objdir / (Path(src).stem + ".o")
+        jobs.append([nvcc, *NVFLAGS, "-c", str(CSRC / src), "-o", str(obj)])
+    for src in C_SOURCES:
+        obj = objdir / (Path(src).stem + ".o")
+        jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-I", str(ROOT / "include"), "-c", str(CSRC / src),
+                     "-o", str(obj)])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and r.stderr:
+            print(r.stderr)
+
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+        list(ex.map(run, jobs))
+    objs = [str(objdir / (Path(s).stem + ".o")) for s in CU_SOURCES + C_SOURCES]
+    tmp = LIB.with_suffix(f".so.{os.getpid()}.tmp")
+    run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"])
+    os.replace(tmp, LIB)
+    # C host driver (drop-in for the reference's main loop)
+    rtmp = RUNNER.with_suffix(f".{os.getpid()}.tmp")
+    run(["gcc", "-O2", "-std=c11", "-I", str(ROOT / "include"), "-o", str(rtmp), str(HOST / "pfdd_run.c"),
+         "-L", str(LIBDIR), "-lpfdd_gb300", f"-Wl,-rpath,{LIBDIR}", "-lm"])
+    os.replace(rtmp, RUNNER)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

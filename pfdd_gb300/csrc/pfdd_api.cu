@@ -1,0 +1,648 @@
+// pfdd_api.cu -- C ABI of the PFDD TDGL hot path (include/pfdd_gpu.h).
+//
+// A context owns, on one GPU and one CUDA stream, everything a solve (or a
+// batch of replicas sharing B(k)) needs between steps: the FP64 state xi,
+// the spectral buffer S, the packed B(k), the pinned-point bit mask, the
+// per-step stress table and the gamma partial sums.  Nothing is copied
+// between host and device inside a step; pfdd_step uploads the stresses of a
+// chunk of steps once and reads back gamma once per chunk.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/pfdd_gpu.h"
+#include "pfdd_kernels.cuh"
+
+using namespace pfdd;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+bool pow2_ok(int n) { return n >= 1 && n <= 512 && (n & (n - 1)) == 0; }
+
+struct Geometry {
+  // z-pass
+  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1;
+  size_t zSmem = 0;
+  // strided passes (y: axis 1, x: axis 0)
+  int TI[2] = {1, 1}, threads[2] = {1, 1}, pitch[2] = {1, 1};
+  long long tiles[2] = {1, 1};
+  size_t smem[2] = {0, 0};
+};
+
+Geometry make_geometry(int n1, int n2, int n3, size_t vsize) {
+  Geometry g;
+  const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
+  const long long lines = (long long)n1 * n2;
+  int TL = std::max(1, kThreads / team3);
+  while ((long long)TL > lines) TL >>= 1;
+  g.zTL = TL;
+  g.zThreads = TL * team3;
+  g.zPitch = L3 >= 8 ? L3 + 1 : L3;
+  g.zNparts = (int)(lines / TL);
+  g.zSmem = (size_t)TL * g.zPitch * vsize;
+  const int Ls[2] = {n2, n1};
+  const long long inner[2] = {(long long)n3, (long long)n2 * n3};
+  for (int ax = 0; ax < 2; ++ax) {
+    const int L = Ls[ax], E = std::min(8, L), team = L / E;
+    int TI = std::max(1, kThreads / team);
+    while ((long long)TI > inner[ax]) TI >>= 1;
+    g.TI[ax] = TI;
+    g.threads[ax] = TI * team;
+    g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
+    g.tiles[ax] = inner[ax] / TI;
+    g.smem[ax] = (size_t)L * g.pitch[ax] * vsize;
+  }
+  return g;
+}
+
+template <typename T>
+cudaError_t set_smem_attrs(size_t maxsmem) {
+  cudaError_t e = cudaFuncSetAttribute(zpass_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fft_strided_kernel<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fft_strided_kernel<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
+}
+
+}  // namespace
+
+struct pfdd_ctx {
+  int n[3] = {0, 0, 0};
+  int ns = 0, nrep = 0, prec = 0, dev = 0;
+  long long N = 0;
+  cudaStream_t st = nullptr;
+  void *S = nullptr;
+  double2 *xi = nullptr;
+  uint32_t *bc = nullptr;
+  void *B = nullptr;
+  double *tau = nullptr, *part = nullptr, *gam_a = nullptr, *gam = nullptr;
+  double *tau_field = nullptr, *dslip_dev = nullptr;
+  uint8_t *active = nullptr;
+  void *tw[3] = {nullptr, nullptr, nullptr};
+  double *h_gam_a = nullptr, *h_gam = nullptr, *h_tau = nullptr;
+  std::vector<uint8_t> h_active;
+  bool hasB = false, hasParams = false, hasState = false, specValid = false, anyBc = false;
+  double cd2[kMaxNs] = {}, asf[kMaxNs] = {}, dslip[kMaxNs] = {}, uq2 = 1.0;
+  int kchunk = 1;
+  Geometry g;
+  long long launches = 0;
+  std::string err;
+};
+
+struct pfdd_fft_plan {
+  int n[3] = {0, 0, 0};
+  int prec = 0, dev = 0, max_batch = 0;
+  long long N = 0;
+  cudaStream_t st = nullptr;
+  void *buf = nullptr;
+  void *tw[3] = {nullptr, nullptr, nullptr};
+  Geometry g;
+};
+
+static pfdd_status fail(pfdd_ctx *c, pfdd_status s, const char *fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return s;
+}
+
+#define CK(ctx, call)                                                                         \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) {                                                                  \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? PFDD_ENOMEM : PFDD_ECUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                          \
+    }                                                                                         \
+  } while (0)
+
+static size_t vsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double2) : sizeof(float2); }
+static size_t bsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double) : sizeof(float); }
+
+extern "C" size_t pfdd_required_bytes(int n1, int n2, int n3, int ns, int nrep, int precision) {
+  const size_t N = (size_t)n1 * n2 * n3, P = (size_t)ns * (ns + 1) / 2, RF = (size_t)nrep * ns;
+  size_t b = RF * N * (sizeof(double2) + vsize_of(precision));  // xi + S
+  b += P * N * bsize_of(precision);                              // B
+  b += (RF * N + 31) / 32 * 4;                                   // bc mask
+  b += 64u << 20;                                                // partials, tables, slack
+  return b;
+}
+
+extern "C" const char *pfdd_status_string(int s) {
+  switch (s) {
+    case PFDD_OK: return "ok";
+    case PFDD_EINVAL: return "invalid argument";
+    case PFDD_ENOMEM: return "out of memory";
+    case PFDD_ECUDA: return "CUDA error";
+    case PFDD_ETIMEOUT: return "device wait timed out";
+    case PFDD_ENONFINITE: return "state became non-finite";
+    case PFDD_ENOTREADY: return "input not set";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char *pfdd_last_error(const pfdd_ctx *c) { return c ? c->err.c_str() : "null context"; }
+extern "C" long long pfdd_last_launch_count(const pfdd_ctx *c) { return c ? c->launches : 0; }
+
+static cudaError_t make_twiddles(void **tw, const int n[3], int prec, cudaStream_t st) {
+  for (int ax = 0; ax < 3; ++ax) {
+    const int L = n[ax];
+    cudaError_t e = cudaMalloc(&tw[ax], (size_t)std::max(L, 1) * vsize_of(prec));
+    if (e != cudaSuccess) return e;
+    if (prec == PFDD_FP64) twiddle_kernel<double><<<(L + 127) / 128, 128, 0, st>>>(tw[ax], L);
+    else twiddle_kernel<float><<<(L + 127) / 128, 128, 0, st>>>(tw[ax], L);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n3, int ns, int nrep, int precision,
+                                           int device) {
+  if (!out) return PFDD_EINVAL;
+  *out = nullptr;
+  if (!pow2_ok(n1) || !pow2_ok(n2) || !pow2_ok(n3) || ns < 1 || ns > 12 || nrep < 1 ||
+      (precision != PFDD_FP64 && precision != PFDD_FFT_FP32))
+    return PFDD_EINVAL;
+  pfdd_ctx *c = new pfdd_ctx();
+  *out = c;
+  c->n[0] = n1; c->n[1] = n2; c->n[2] = n3;
+  c->ns = ns; c->nrep = nrep; c->prec = precision; c->dev = device;
+  c->N = (long long)n1 * n2 * n3;
+  CK(c, cudaSetDevice(device));
+  CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  c->g = make_geometry(n1, n2, n3, vsize_of(precision));
+  const size_t maxsmem = std::max({c->g.zSmem, c->g.smem[0], c->g.smem[1]});
+  if (precision == PFDD_FP64) CK(c, set_smem_attrs<double>(maxsmem));
+  else CK(c, set_smem_attrs<float>(maxsmem));
+  const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
+  CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
+  CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
+  CK(c, cudaMalloc(&c->B, P * N * bsize_of(precision)));
+  CK(c, cudaMalloc(&c->active, nrep));
+  CK(c, cudaMalloc(&c->dslip_dev, kMaxNs * sizeof(double)));
+  // partial sums for a chunk of steps, bounded to ~32 MB
+  const size_t per_step = RF * (size_t)c->g.zNparts;
+  c->kchunk = (int)std::max<size_t>(1, std::min<size_t>(1024, (4u << 20) / std::max<size_t>(per_step, 1)));
+  CK(c, cudaMalloc(&c->part, per_step * c->kchunk * sizeof(double)));
+  CK(c, cudaMalloc(&c->tau, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, cudaMalloc(&c->gam_a, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, cudaMalloc(&c->gam, (size_t)c->kchunk * nrep * sizeof(double)));
+  CK(c, cudaMallocHost(&c->h_gam_a, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, cudaMallocHost(&c->h_gam, (size_t)c->kchunk * nrep * sizeof(double)));
+  CK(c, cudaMallocHost(&c->h_tau, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, make_twiddles(c->tw, c->n, precision, c->st));
+  c->h_active.assign(nrep, 1);
+  CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), nrep, cudaMemcpyHostToDevice, c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_create(pfdd_ctx **out, int n1, int n2, int n3, int ns, int precision, int device) {
+  return pfdd_create_batched(out, n1, n2, n3, ns, 1, precision, device);
+}
+
+extern "C" void pfdd_destroy(pfdd_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->dev);
+  if (c->st) cudaStreamSynchronize(c->st);
+  void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
+                c->active, c->tw[0], c->tw[1], c->tw[2]};
+  for (void *p : dp)
+    if (p) cudaFree(p);
+  if (c->h_gam_a) cudaFreeHost(c->h_gam_a);
+  if (c->h_gam) cudaFreeHost(c->h_gam);
+  if (c->h_tau) cudaFreeHost(c->h_tau);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+extern "C" pfdd_status pfdd_set_B(pfdd_ctx *c, const double *B) {
+  if (!c || !B) return fail(c, PFDD_EINVAL, "pfdd_set_B: null argument");
+  CK(c, cudaSetDevice(c->dev));
+  const size_t full = (size_t)c->ns * c->ns * c->N * sizeof(double);
+  double *tmp = nullptr;
+  CK(c, cudaMalloc(&tmp, full));
+  cudaError_t e = cudaMemcpyAsync(tmp, B, full, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) {
+    pack_B_kernel<<<1216, kThreads, 0, c->st>>>(tmp, c->ns, c->N, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
+                                                 c->prec == PFDD_FP64 ? nullptr : (float *)c->B);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(tmp);
+  CK(c, e);
+  c->hasB = true;
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_get_B(pfdd_ctx *c, double *B) {
+  if (!c || !B) return fail(c, PFDD_EINVAL, "pfdd_get_B: null argument");
+  if (!c->hasB) return fail(c, PFDD_ENOTREADY, "pfdd_get_B: B(k) not set");
+  CK(c, cudaSetDevice(c->dev));
+  const size_t full = (size_t)c->ns * c->ns * c->N * sizeof(double);
+  double *tmp = nullptr;
+  CK(c, cudaMalloc(&tmp, full));
+  unpack_B_kernel<<<1216, kThreads, 0, c->st>>>(c->prec == PFDD_FP64 ? (const double *)c->B : nullptr,
+                                                c->prec == PFDD_FP64 ? nullptr : (const float *)c->B, c->ns, c->N, tmp);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B, tmp, full, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(tmp);
+  CK(c, e);
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double C44, const double *eps, double d1,
+                                    double d2, double d3) {
+  if (!c || !eps) return fail(c, PFDD_EINVAL, "pfdd_build_B: null argument");
+  if (!(C44 != 0.0) || !(d1 > 0) || !(d2 > 0) || !(d3 > 0)) return fail(c, PFDD_EINVAL, "pfdd_build_B: bad constants");
+  CK(c, cudaSetDevice(c->dev));
+  BBuildParams hp;
+  std::memset(&hp, 0, sizeof hp);
+  hp.n1 = c->n[0]; hp.n2 = c->n[1]; hp.n3 = c->n[2]; hp.ns = c->ns;
+  hp.d1 = d1; hp.d2 = d2; hp.d3 = d3;
+  hp.mu = C44; hp.ll = C12; hp.mup = C11 - C12 - 2 * C44; hp.mu_inv = 1. / hp.mu;
+  // C_ijkl of Bmatrix (F:347-357), sigma_a = C : eps_a, E_ab = eps_a : C : eps_b
+  double Cc[3][3][3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k)
+        for (int m = 0; m < 3; ++m)
+          Cc[i][j][k][m] = hp.mu * ((i == k) * (j == m) + (i == m) * (j == k)) + hp.ll * (i == j) * (k == m) +
+                           hp.mup * ((i == j) && (j == k) && (k == m));
+  for (int a = 0; a < c->ns; ++a)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double s = 0;
+        for (int m = 0; m < 3; ++m)
+          for (int n = 0; n < 3; ++n) s += Cc[i][j][m][n] * eps[(a * 3 + m) * 3 + n];
+        hp.sig[a][i][j] = s;
+      }
+  for (int a = 0; a < c->ns; ++a)
+    for (int b = 0; b < c->ns; ++b) {
+      double s = 0;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) s += eps[(a * 3 + i) * 3 + j] * hp.sig[b][i][j];
+      hp.E[a][b] = s;
+    }
+  BBuildParams *dp = nullptr;
+  CK(c, cudaMalloc(&dp, sizeof hp));
+  cudaError_t e = cudaMemcpyAsync(dp, &hp, sizeof hp, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) {
+    build_B_kernel<<<1216, 128, 0, c->st>>>(dp, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
+                                            c->prec == PFDD_FP64 ? nullptr : (float *)c->B, c->N);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(dp);
+  CK(c, e);
+  c->hasB = true;
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_set_params(pfdd_ctx *c, const double *cd2, const double *asf, const double *dslip,
+                                       double uq2) {
+  if (!c || !cd2 || !asf || !dslip) return fail(c, PFDD_EINVAL, "pfdd_set_params: null argument");
+  for (int a = 0; a < c->ns; ++a) {
+    if (!(dslip[a] != 0.0)) return fail(c, PFDD_EINVAL, "pfdd_set_params: dslip[%d] == 0", a);
+    c->cd2[a] = cd2[a]; c->asf[a] = asf[a]; c->dslip[a] = dslip[a];
+  }
+  c->uq2 = uq2;
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaMemcpyAsync(c->dslip_dev, c->dslip, sizeof(double) * kMaxNs, cudaMemcpyHostToDevice, c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  c->hasParams = true;
+  return PFDD_OK;
+}
+
+// Upload xi (and the pinned mask) of replicas [r0, r0+nr).
+static pfdd_status upload_state(pfdd_ctx *c, int r0, int nr, const double *xi, const double *bc) {
+  CK(c, cudaSetDevice(c->dev));
+  const size_t fieldN = (size_t)c->N, RFn = (size_t)nr * c->ns;
+  CK(c, cudaMemcpyAsync(c->xi + (size_t)r0 * c->ns * fieldN, xi, RFn * fieldN * sizeof(double2),
+                        cudaMemcpyHostToDevice, c->st));
+  // pinned mask: bit set where xi_bc[..][0] != 0 (the reference tests == 0 to evolve, F:3481)
+  bool any = false;
+  if (bc)
+    for (size_t e = 0; e < RFn * fieldN && !any; ++e) any = bc[2 * e] != 0.0;
+  const size_t total_bits = (size_t)c->nrep * c->ns * fieldN, words = (total_bits + 31) / 32;
+  if (any && !c->bc) {
+    CK(c, cudaMalloc(&c->bc, words * 4));
+    CK(c, cudaMemsetAsync(c->bc, 0, words * 4, c->st));
+  }
+  if (c->bc) {
+    // rebuild the words of this replica range on the host (range is word-aligned only
+    // when ns*N is a multiple of 32, so read-modify-write the whole mask)
+    std::vector<uint32_t> m(words);
+    CK(c, cudaMemcpyAsync(m.data(), c->bc, words * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaStreamSynchronize(c->st));
+    const size_t b0 = (size_t)r0 * c->ns * fieldN;
+    for (size_t e = 0; e < RFn * fieldN; ++e) {
+      const size_t bit = b0 + e;
+      const bool pin = bc && bc[2 * e] != 0.0;
+      if (pin) m[bit >> 5] |= (1u << (bit & 31));
+      else m[bit >> 5] &= ~(1u << (bit & 31));
+    }
+    CK(c, cudaMemcpyAsync(c->bc, m.data(), words * 4, cudaMemcpyHostToDevice, c->st));
+  }
+  CK(c, cudaStreamSynchronize(c->st));
+  c->hasState = true;
+  c->specValid = false;
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_set_state(pfdd_ctx *c, const double *xi, const double *bc) {
+  if (!c || !xi) return fail(c, PFDD_EINVAL, "pfdd_set_state: null argument");
+  return upload_state(c, 0, c->nrep, xi, bc);
+}
+
+extern "C" pfdd_status pfdd_set_replica_state(pfdd_ctx *c, int r, const double *xi, const double *bc) {
+  if (!c || !xi || r < 0 || r >= c->nrep) return fail(c, PFDD_EINVAL, "pfdd_set_replica_state: bad argument");
+  return upload_state(c, r, 1, xi, bc);
+}
+
+extern "C" pfdd_status pfdd_set_tau_field(pfdd_ctx *c, const double *tf) {
+  if (!c) return PFDD_EINVAL;
+  CK(c, cudaSetDevice(c->dev));
+  if (!tf) {
+    if (c->tau_field) CK(c, cudaFree(c->tau_field));
+    c->tau_field = nullptr;
+    return PFDD_OK;
+  }
+  const size_t N = (size_t)c->N, ns = (size_t)c->ns;
+  std::vector<double> t(ns * N);
+  for (size_t pt = 0; pt < N; ++pt)
+    for (size_t a = 0; a < ns; ++a) t[a * N + pt] = tf[pt * ns + a];
+  if (!c->tau_field) CK(c, cudaMalloc(&c->tau_field, ns * N * sizeof(double)));
+  CK(c, cudaMemcpyAsync(c->tau_field, t.data(), ns * N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_set_replica_active(pfdd_ctx *c, int r, int on) {
+  if (!c || r < 0 || r >= c->nrep) return fail(c, PFDD_EINVAL, "pfdd_set_replica_active: bad replica");
+  c->h_active[r] = on ? 1 : 0;
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), c->nrep, cudaMemcpyHostToDevice, c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  return PFDD_OK;
+}
+
+template <typename T>
+static cudaError_t launch_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
+  zp.flags = flags;
+  const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
+  zpass_kernel<T><<<(unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st>>>(zp);
+  c->launches++;
+  return cudaGetLastError();
+}
+
+template <typename T, int S>
+static cudaError_t launch_strided(pfdd_ctx *c, int ax /*0: y, 1: x*/) {
+  const int L = ax == 0 ? c->n[1] : c->n[0];
+  if (L == 1) return cudaSuccess;
+  const int gi = ax == 0 ? 0 : 1;
+  const long long inner = ax == 0 ? (long long)c->n[2] : (long long)c->n[1] * c->n[2];
+  const long long outer = ax == 0 ? (long long)c->nrep * c->ns * c->n[0] : (long long)c->nrep * c->ns;
+  const long long outer_per_rep = outer / c->nrep;
+  const long long blocks = outer * c->g.tiles[gi];
+  fft_strided_kernel<T, S><<<(unsigned)blocks, c->g.threads[gi], c->g.smem[gi], c->st>>>(
+      c->S, L, inner, c->g.TI[gi], c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0], c->active, outer_per_rep, c->g.pitch[gi]);
+  c->launches++;
+  return cudaGetLastError();
+}
+
+template <typename T, int NS>
+static cudaError_t launch_contract_ns(pfdd_ctx *c) {
+  const int blocks = (int)std::min<long long>((c->N + kThreads - 1) / kThreads, 152LL * 8);
+  // FP32 batches: 2-4 replicas per pass reuse each loaded B value (register budget
+  // allows 4 for NS <= 4, 2 up to NS = 12); FP64 keeps one replica per pass.
+  constexpr int RCF = std::is_same<T, float>::value ? (NS <= 4 ? 4 : 2) : 1;
+  if (RCF > 1 && c->nrep > 1)
+    contract_kernel<T, NS, RCF><<<blocks, kThreads, 0, c->st>>>(c->S, (const T *)c->B, c->N, c->nrep, c->active);
+  else
+    contract_kernel<T, NS, 1><<<blocks, kThreads, 0, c->st>>>(c->S, (const T *)c->B, c->N, c->nrep, c->active);
+  c->launches++;
+  return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t launch_contract(pfdd_ctx *c) {
+  switch (c->ns) {
+    case 1: return launch_contract_ns<T, 1>(c);
+    case 2: return launch_contract_ns<T, 2>(c);
+    case 3: return launch_contract_ns<T, 3>(c);
+    case 4: return launch_contract_ns<T, 4>(c);
+    case 5: return launch_contract_ns<T, 5>(c);
+    case 6: return launch_contract_ns<T, 6>(c);
+    case 7: return launch_contract_ns<T, 7>(c);
+    case 8: return launch_contract_ns<T, 8>(c);
+    case 9: return launch_contract_ns<T, 9>(c);
+    case 10: return launch_contract_ns<T, 10>(c);
+    case 11: return launch_contract_ns<T, 11>(c);
+    case 12: return launch_contract_ns<T, 12>(c);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T>
+static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double *gamma, double *gamma_a) {
+  ZParams zp;
+  std::memset(&zp, 0, sizeof zp);
+  zp.S = c->S; zp.xi = c->xi; zp.bc = c->bc; zp.tau = c->tau; zp.tau_field = c->tau_field;
+  zp.dslip = c->dslip_dev; zp.part = c->part;
+  zp.active = c->active;
+  zp.tw = c->tw[2];
+  zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
+  zp.L = c->n[2]; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
+  zp.pitch = c->g.zPitch;
+  zp.inv_n = 1.0 / (double)c->N;  // N is a power of two: exact, same as dividing by nsize
+  zp.uq2 = c->uq2;
+  for (int a = 0; a < c->ns; ++a) {
+    zp.cd2[a] = c->cd2[a];
+    zp.asf_pi[a] = c->asf[a] * kPiTrunc;  // Asf2[isa]*pi, F:3488
+    zp.uq2cd2[a] = c->uq2 * c->cd2[a];    // uq2*CD2[isa], F:3489
+  }
+  const int RF = c->nrep * c->ns;
+  if (!c->specValid) {
+    CK(c, launch_zpass<T>(c, zp, Z_SRC_XI | Z_FWD | Z_STORE));
+    c->specValid = true;
+  }
+  for (int s0 = 0; s0 < nsteps; s0 += c->kchunk) {
+    const int ks = std::min(c->kchunk, nsteps - s0);
+    // per-step stress table: tau/dslip (F:3488) or the tau-field multiplier
+    for (int s = 0; s < ks; ++s)
+      for (int r = 0; r < c->nrep; ++r)
+        for (int a = 0; a < c->ns; ++a) {
+          const double t = tau[((size_t)(s0 + s) * c->nrep + r) * c->ns + a];
+          c->h_tau[((size_t)s * c->nrep + r) * c->ns + a] = c->tau_field ? t : t / c->dslip[a];
+        }
+    CK(c, cudaMemcpyAsync(c->tau, c->h_tau, (size_t)ks * RF * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    for (int s = 0; s < ks; ++s) {
+      CK(c, (launch_strided<T, -1>(c, 0)));
+      CK(c, (launch_strided<T, -1>(c, 1)));
+      CK(c, launch_contract<T>(c));
+      CK(c, (launch_strided<T, +1>(c, 1)));
+      CK(c, (launch_strided<T, +1>(c, 0)));
+      zp.step = s;
+      CK(c, launch_zpass<T>(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE));
+    }
+    const int nt = ks * c->nrep;
+    gamma_reduce_kernel<<<(nt + 127) / 128, 128, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, ks, zp.inv_n,
+                                                             c->gam_a, c->gam);
+    c->launches++;
+    CK(c, cudaGetLastError());
+    CK(c, cudaMemcpyAsync(c->h_gam_a, c->gam_a, (size_t)ks * RF * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaMemcpyAsync(c->h_gam, c->gam, (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaStreamSynchronize(c->st));
+    bool finite = true;
+    for (int q = 0; q < nt; ++q)
+      if (c->h_active[q % c->nrep] && !std::isfinite(c->h_gam[q])) finite = false;
+    if (gamma) std::memcpy(gamma + (size_t)s0 * c->nrep, c->h_gam, (size_t)nt * sizeof(double));
+    if (gamma_a) std::memcpy(gamma_a + (size_t)s0 * RF, c->h_gam_a, (size_t)ks * RF * sizeof(double));
+    if (!finite) return fail(c, PFDD_ENONFINITE, "pfdd_step: state became non-finite within steps %d..%d", s0, s0 + ks - 1);
+  }
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_step(pfdd_ctx *c, int nsteps, const double *tau, double *gamma, double *gamma_a) {
+  if (!c || nsteps < 0 || (nsteps > 0 && !tau)) return fail(c, PFDD_EINVAL, "pfdd_step: bad argument");
+  if (!c->hasB) return fail(c, PFDD_ENOTREADY, "pfdd_step: B(k) not set");
+  if (!c->hasParams) return fail(c, PFDD_ENOTREADY, "pfdd_step: parameters not set");
+  if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_step: state not set");
+  c->launches = 0;
+  if (nsteps == 0) return PFDD_OK;
+  CK(c, cudaSetDevice(c->dev));
+  return c->prec == PFDD_FP64 ? run_steps<double>(c, nsteps, tau, gamma, gamma_a)
+                              : run_steps<float>(c, nsteps, tau, gamma, gamma_a);
+}
+
+extern "C" pfdd_status pfdd_get_state(pfdd_ctx *c, double *xi) {
+  if (!c || !xi) return fail(c, PFDD_EINVAL, "pfdd_get_state: null argument");
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaMemcpyAsync(xi, c->xi, (size_t)c->nrep * c->ns * c->N * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_get_replica_state(pfdd_ctx *c, int r, double *xi) {
+  if (!c || !xi || r < 0 || r >= c->nrep) return fail(c, PFDD_EINVAL, "pfdd_get_replica_state: bad argument");
+  CK(c, cudaSetDevice(c->dev));
+  const size_t fl = (size_t)c->ns * c->N;
+  CK(c, cudaMemcpyAsync(xi, c->xi + (size_t)r * fl, fl * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  return PFDD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FFT boundary (fft_forward / fft_backward of F:209-273)
+
+extern "C" pfdd_status pfdd_fft_plan_create(pfdd_fft_plan **out, int n1, int n2, int n3, int precision,
+                                            int max_batch, int device) {
+  if (!out) return PFDD_EINVAL;
+  *out = nullptr;
+  if (!pow2_ok(n1) || !pow2_ok(n2) || !pow2_ok(n3) || max_batch < 1 ||
+      (precision != PFDD_FP64 && precision != PFDD_FFT_FP32))
+    return PFDD_EINVAL;
+  pfdd_fft_plan *p = new pfdd_fft_plan();
+  p->n[0] = n1; p->n[1] = n2; p->n[2] = n3;
+  p->prec = precision; p->dev = device; p->max_batch = max_batch;
+  p->N = (long long)n1 * n2 * n3;
+  p->g = make_geometry(n1, n2, n3, vsize_of(precision));
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->st, cudaStreamNonBlocking);
+  const size_t maxsmem = std::max({p->g.zSmem, p->g.smem[0], p->g.smem[1]});
+  if (e == cudaSuccess) e = precision == PFDD_FP64 ? set_smem_attrs<double>(maxsmem) : set_smem_attrs<float>(maxsmem);
+  if (e == cudaSuccess) e = cudaMalloc(&p->buf, (size_t)max_batch * p->N * vsize_of(precision));
+  if (e == cudaSuccess) e = make_twiddles(p->tw, p->n, precision, p->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  if (e != cudaSuccess) {
+    pfdd_fft_plan_destroy(p);
+    return e == cudaErrorMemoryAllocation ? PFDD_ENOMEM : PFDD_ECUDA;
+  }
+  *out = p;
+  return PFDD_OK;
+}
+
+extern "C" void pfdd_fft_plan_destroy(pfdd_fft_plan *p) {
+  if (!p) return;
+  cudaSetDevice(p->dev);
+  if (p->st) cudaStreamSynchronize(p->st);
+  if (p->buf) cudaFree(p->buf);
+  for (void *t : p->tw)
+    if (t) cudaFree(t);
+  if (p->st) cudaStreamDestroy(p->st);
+  delete p;
+}
+
+template <typename T>
+static cudaError_t fft_exec(pfdd_fft_plan *p, void *dbuf, int batch, int sign) {
+  const Geometry &g = p->g;
+  ZParams zp;
+  std::memset(&zp, 0, sizeof zp);
+  zp.S = dbuf; zp.tw = p->tw[2]; zp.N = p->N; zp.lines_per_field = (long long)p->n[0] * p->n[1];
+  zp.L = p->n[2]; zp.ns = batch; zp.R = 1; zp.TL = g.zTL; zp.nparts = g.zNparts; zp.pitch = g.zPitch;
+  const long long zblocks = (long long)batch * g.zNparts;
+  auto strided = [&](int ax, int s) -> cudaError_t {
+    const int L = ax == 0 ? p->n[1] : p->n[0];
+    if (L == 1) return cudaSuccess;
+    const int gi = ax == 0 ? 0 : 1;
+    const long long inner = ax == 0 ? (long long)p->n[2] : (long long)p->n[1] * p->n[2];
+    const long long outer = ax == 0 ? (long long)batch * p->n[0] : (long long)batch;
+    const long long blocks = outer * g.tiles[gi];
+    if (s < 0)
+      fft_strided_kernel<T, -1><<<(unsigned)blocks, g.threads[gi], g.smem[gi], p->st>>>(
+          dbuf, L, inner, g.TI[gi], g.tiles[gi], p->tw[ax == 0 ? 1 : 0], nullptr, outer, g.pitch[gi]);
+    else
+      fft_strided_kernel<T, +1><<<(unsigned)blocks, g.threads[gi], g.smem[gi], p->st>>>(
+          dbuf, L, inner, g.TI[gi], g.tiles[gi], p->tw[ax == 0 ? 1 : 0], nullptr, outer, g.pitch[gi]);
+    return cudaGetLastError();
+  };
+  cudaError_t e;
+  if (sign < 0) {
+    zp.flags = Z_FWD | Z_STORE;
+    zpass_kernel<T><<<(unsigned)zblocks, g.zThreads, g.zSmem, p->st>>>(zp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = strided(0, -1)) != cudaSuccess) return e;
+    return strided(1, -1);
+  }
+  if ((e = strided(1, +1)) != cudaSuccess) return e;
+  if ((e = strided(0, +1)) != cudaSuccess) return e;
+  zp.flags = Z_INV | Z_STORE;
+  zpass_kernel<T><<<(unsigned)zblocks, g.zThreads, g.zSmem, p->st>>>(zp);
+  return cudaGetLastError();
+}
+
+static pfdd_status fft_call(pfdd_fft_plan *p, void *data, int batch, int on_device, int sign) {
+  if (!p || !data || batch < 1 || batch > p->max_batch) return PFDD_EINVAL;
+  if (cudaSetDevice(p->dev) != cudaSuccess) return PFDD_ECUDA;
+  const size_t bytes = (size_t)batch * p->N * vsize_of(p->prec);
+  void *d = on_device ? data : p->buf;
+  cudaError_t e = cudaSuccess;
+  if (!on_device) e = cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, p->st);
+  if (e == cudaSuccess) e = p->prec == PFDD_FP64 ? fft_exec<double>(p, d, batch, sign) : fft_exec<float>(p, d, batch, sign);
+  if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, p->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  return e == cudaSuccess ? PFDD_OK : PFDD_ECUDA;
+}
+
+extern "C" pfdd_status pfdd_fft_forward(pfdd_fft_plan *p, void *data, int batch, int on_device) {
+  return fft_call(p, data, batch, on_device, -1);
+}
+extern "C" pfdd_status pfdd_fft_backward(pfdd_fft_plan *p, void *data, int batch, int on_device) {
+  return fft_call(p, data, batch, on_device, +1);
+}

@@ -1,0 +1,124 @@
+/*
+ * pfdd_run.c -- C host driver: the reference program's TDGL loop on the GPU.
+ *
+ * Mirrors the hot path of `main` in PFDD_Final_GPU.c (F:4087-4847) for a
+ * homogeneous FCC crystal: reads xi.dat / xi_bc.dat (F:4366-4382, choice==2),
+ * builds the slip systems (setfcc F:1812-1909, setorient F:1987-2057, seteps
+ * F:1912-1980), the resolved shear stress of an applied sigma_xz (resolSS
+ * F:1540-1637), builds B(k) on the GPU (Bmatrix F:328-412), runs K TDGL steps
+ * with a linear stress ramp (plasticevolv F:3470-3501, loop F:4574-4691),
+ * and writes phasefield.dat (F:4672), gamma_full.dat (full precision) and
+ * xi.dat (F:4777-4788) in the working directory.
+ *
+ * usage: pfdd_run N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C]
+ *                 [--mu MU] [--lambda LAM] [--bdiv BD] [--fp32] [--device D]
+ *
+ * NSF (default NS) is the slip-system count of the files; systems NS..NSF-1
+ * and the 9 virtual-strain fields must be zero and pinned (they contribute
+ * nothing to the force and never evolve).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/time.h>
+
+#include "pfdd_gpu.h"
+#include "pfdd_setup.h"
+
+static double wtime(void) {
+  struct timeval tv;
+  gettimeofday(&tv, NULL);
+  return tv.tv_sec + tv.tv_usec / 1e6;
+}
+
+static int die(const char *msg, pfdd_ctx *c, int st) {
+  fprintf(stderr, "pfdd_run: %s: %s %s\n", msg, pfdd_status_string(st), c ? pfdd_last_error(c) : "");
+  return 1;
+}
+
+int main(int argc, char **argv) {
+  if (argc < 7) {
+    fprintf(stderr, "usage: %s N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C] [--mu MU] [--lambda LAM] "
+                    "[--bdiv BD] [--fp32] [--device D]\n", argv[0]);
+    return 2;
+  }
+  int n1 = atoi(argv[1]), n2 = atoi(argv[2]), n3 = atoi(argv[3]), ns = atoi(argv[4]), K = atoi(argv[5]);
+  double sigma_max = atof(argv[6]);
+  int nsf = ns, prec = PFDD_FP64, dev = 0;
+  double asf = 0.1, cd2 = 0.01, mu = 1.0, lam = 1.5, bdiv = sqrt(2.0);
+  for (int i = 7; i < argc; ++i) {
+    if (!strcmp(argv[i], "--nsfile") && i + 1 < argc) nsf = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--asf") && i + 1 < argc) asf = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--cd2") && i + 1 < argc) cd2 = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--mu") && i + 1 < argc) mu = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--lambda") && i + 1 < argc) lam = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--bdiv") && i + 1 < argc) bdiv = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--fp32")) prec = PFDD_FFT_FP32;
+    else if (!strcmp(argv[i], "--device") && i + 1 < argc) dev = atoi(argv[++i]);
+    else { fprintf(stderr, "unknown option %s\n", argv[i]); return 2; }
+  }
+  if (ns < 1 || ns > 12 || nsf < ns || K < 1) { fprintf(stderr, "bad NS/K\n"); return 2; }
+  const long N = (long)n1 * n2 * n3;
+  const int nsv = nsf + 9;
+  const size_t cnt = (size_t)2 * nsv * N;
+  double *xi = malloc(cnt * sizeof(double)), *bc = malloc(cnt * sizeof(double));
+  if (!xi || !bc) { fprintf(stderr, "out of host memory\n"); return 1; }
+  FILE *fx = fopen("xi.dat", "rb"), *fb = fopen("xi_bc.dat", "rb");
+  if (!fx || !fb || fread(xi, sizeof(double), cnt, fx) != cnt || fread(bc, sizeof(double), cnt, fb) != cnt) {
+    fprintf(stderr, "cannot read xi.dat / xi_bc.dat of %zu doubles\n", cnt);
+    return 1;
+  }
+  fclose(fx); fclose(fb);
+  for (size_t e = (size_t)2 * ns * N; e < cnt; ++e)
+    if (xi[e] != 0.0 || bc[e - (e & 1)] == 0.0) {
+      fprintf(stderr, "fields beyond the first %d slip systems must be zero and pinned\n", ns);
+      return 1;
+    }
+
+  /* setup (F:4253-4330) */
+  double C44 = mu, C12 = lam, C11 = 2. * C44 + C12; /* isotropic: C11 = 2 C44 + C12, F:4243-4245 */
+  double xn[12][3], xb[12][3], th[3][3], dslip[12], eps[12][3][3], tau_max[12];
+  for (int s = 0; s < 12; ++s) dslip[s] = 1.0;
+  pfdd_setfcc(xn, xb, bdiv);
+  pfdd_setorient(th);
+  pfdd_seteps(12, (const double(*)[3])xn, (const double(*)[3])xb, dslip, (const double(*)[3])th, eps);
+  double sig[3][3] = {{0, 0, sigma_max}, {0, 0, 0}, {sigma_max, 0, 0}};
+  pfdd_resolve_shear(ns, (const double(*)[3])sig, (const double(*)[3][3])eps, tau_max);
+  double *tau = malloc(sizeof(double) * (size_t)K * ns);
+  pfdd_ramp_tau(ns, tau_max, K, tau);
+  double cdv[12], asfv[12];
+  for (int s = 0; s < 12; ++s) { cdv[s] = cd2; asfv[s] = asf; }
+
+  pfdd_ctx *c = NULL;
+  int st;
+  double t0 = wtime();
+  if ((st = pfdd_create(&c, n1, n2, n3, ns, prec, dev)) != PFDD_OK) return die("create", c, st);
+  if ((st = pfdd_build_B(c, C11, C12, C44, &eps[0][0][0], 1.0, 1.0, 1.0)) != PFDD_OK) return die("build_B", c, st);
+  if ((st = pfdd_set_params(c, cdv, asfv, dslip, 1.0)) != PFDD_OK) return die("set_params", c, st);
+  if ((st = pfdd_set_state(c, xi, bc)) != PFDD_OK) return die("set_state", c, st);
+  double *gamma = malloc(sizeof(double) * K), *gamma_a = malloc(sizeof(double) * (size_t)K * ns);
+  double t1 = wtime();
+  if ((st = pfdd_step(c, K, tau, gamma, gamma_a)) != PFDD_OK) return die("step", c, st);
+  double t2 = wtime();
+  if ((st = pfdd_get_state(c, xi)) != PFDD_OK) return die("get_state", c, st);
+
+  FILE *pf = fopen("phasefield.dat", "w"), *gf = fopen("gamma_full.dat", "w");
+  for (int s = 0; s < K; ++s) {
+    /* it = 1: the single outer step that runs the inner loop; it_plastic counts from 1 */
+    fprintf(pf, "%d       %d         %e           %e           %e\n", 1, s + 1, gamma_a[(size_t)s * ns],
+            ns > 1 ? gamma_a[(size_t)s * ns + 1] : 0.0, gamma[s]);
+    fprintf(gf, "%d %.17e", s + 1, gamma[s]);
+    for (int a = 0; a < ns; ++a) fprintf(gf, " %.17e", gamma_a[(size_t)s * ns + a]);
+    fprintf(gf, "\n");
+  }
+  fclose(pf); fclose(gf);
+  FILE *fo = fopen("xi.dat", "r+b");
+  if (!fo || fwrite(xi, sizeof(double), cnt, fo) != cnt) { fprintf(stderr, "cannot write xi.dat\n"); return 1; }
+  fclose(fo);
+  printf("pfdd_run: %dx%dx%d ns=%d K=%d %s setup %.3fs steps %.3fs (%.1f steps/s)\n", n1, n2, n3, ns, K,
+         prec == PFDD_FP64 ? "fp64" : "fp32", t1 - t0, t2 - t1, K / (t2 - t1));
+  pfdd_destroy(c);
+  free(xi); free(bc); free(tau); free(gamma); free(gamma_a);
+  return 0;
+}

@@ -1,0 +1,39 @@
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 (runs the CUDA path)")
+
+
+@pytest.fixture(scope="session")
+def native_lib():
+    """The in-tree native library, (re)built if its sources changed."""
+    from pfdd_gb300 import build, native
+    build.build()
+    return native.load()
+
+
+def golden_cases():
+    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+def load_golden(name):
+    from pfdd_gb300 import workloads
+    z = np.load(GOLDEN / f"{name}.npz")
+    d = json.loads(str(z["spec"]))
+    d["loops"] = [workloads.Loop(lp["system"], tuple(lp["center"]), lp["radius"]) for lp in d["loops"]]
+    d["n"] = tuple(d["n"])
+    d["d"] = tuple(d["d"])
+    spec = workloads.SolveSpec(**d)
+    return spec, z

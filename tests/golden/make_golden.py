@@ -1,0 +1,103 @@
+"""Generate the golden vectors in tests/golden/ by running the patched reference program.
+
+Run here (where the reference checkout exists): ``python tests/golden/make_golden.py``.
+For every case it builds the patched reference (oracle/build_ref.py) in FP64
+(``-Dfloat=double``, the reference's own double-precision run) and in its stock FP32
+spectral precision, writes the seeded inputs as xi.dat / xi_bc.dat (the reference is
+built with 12 FCC systems; systems beyond the case's ``ns`` are zero and pinned), runs
+it, and stores per-step gamma / gamma_a (full precision) and the final xi (full field
+for small grids, a seeded sample of points otherwise) in ``<case>.npz``.
+"""
+from __future__ import annotations
+
+import json
+import shutil
+import sys
+import tempfile
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import asdict
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+import build_ref  # noqa: E402
+from pfdd_gb300 import refio, workloads  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+FULL_LIMIT = 8192  # grids up to this many points store the full final field
+
+
+def cases():
+    c0 = workloads.config0()
+    yield "config0_32c_ns3_k200", c0
+    yield "fcc12_8x16x32_k40", workloads.SolveSpec(
+        n=(8, 16, 32), ns=12, steps=40, sigma_max=0.05,
+        loops=workloads.random_loops((8, 16, 32), 4, 2.0, 5.0, 12, seed=7), noise_seed=7)
+    yield "quasi2d_32x2x32_ns3_k50", workloads.SolveSpec(
+        n=(32, 2, 32), ns=3, steps=50, sigma_max=0.03,
+        loops=[workloads.Loop(0, (16, 0, 16), 6.0), workloads.Loop(1, (10, 1, 8), 4.0)], noise_seed=3)
+    yield "fcc12_8c_k30", workloads.SolveSpec(
+        n=(8, 8, 8), ns=12, steps=30, sigma_max=0.08,
+        loops=workloads.random_loops((8, 8, 8), 3, 1.5, 3.0, 12, seed=11), noise_seed=11)
+    yield "config1_64c_ns12_k10", workloads.config1(steps=10, n=64)
+
+
+def spec_json(spec: workloads.SolveSpec) -> str:
+    d = asdict(spec)
+    return json.dumps(d)
+
+
+def run_case(name: str, spec: workloads.SolveSpec, fp64: bool):
+    b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=fp64,
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
+    d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
+    try:
+        xi, bc = workloads.initial_state(spec)
+        refio.write_xi_files(d, xi, bc, ns_ref=12)
+        build_ref.run_ref(b, d)
+        g = refio.read_gamma_full(d / "gamma_full.dat")
+        xf = refio.read_xi_file(d / "xi.dat", spec.n, 12 + refio.NV)
+        return g, xf[:spec.ns]
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def sample_points(npts: int, count: int, seed: int) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return np.sort(rng.choice(npts, size=min(count, npts), replace=False))
+
+
+def make(name: str, spec: workloads.SolveSpec):
+    with ThreadPoolExecutor(2) as ex:
+        f64 = ex.submit(run_case, name, spec, True)
+        f32 = ex.submit(run_case, name, spec, False)
+        (g64, x64), (g32, x32) = f64.result(), f32.result()
+    K = spec.steps
+    assert g64.shape[0] == K, f"{name}: reference stopped after {g64.shape[0]} steps"
+    npts = spec.npts
+    xi0, _ = workloads.initial_state(spec)
+    out = dict(spec=spec_json(spec), gamma=g64[:, 1], gamma_a=g64[:, 2:2 + spec.ns],
+               gamma_fp32ref=g32[:, 1], gamma_a_fp32ref=g32[:, 2:2 + spec.ns],
+               xi0_checksum=np.array([xi0.real.sum(), (xi0.real ** 2).sum()]),
+               xi_final_checksum=np.array([x64.real.sum(), x64.imag.sum(), (np.abs(x64) ** 2).sum()]),
+               fp32ref_max_dxi=np.array(np.max(np.abs(x32 - x64))))
+    flat = x64.reshape(spec.ns, -1)
+    if npts <= FULL_LIMIT:
+        out["xi_final"] = flat
+    else:
+        idx = sample_points(npts, 2048, seed=12345)
+        out["sample_idx"] = idx
+        out["xi_final_sample"] = flat[:, idx]
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print(f"{name}: K={K} gamma[-1]={g64[-1, 1]:.6e} fp32-ref max|dxi|={float(out['fp32ref_max_dxi']):.2e}")
+
+
+if __name__ == "__main__":
+    want = set(sys.argv[1:])
+    for nm, sp in cases():
+        if not want or nm in want:
+            make(nm, sp)

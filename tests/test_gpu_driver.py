@@ -1,0 +1,40 @@
+"""The C host driver (reads xi.dat/xi_bc.dat, writes phasefield.dat / xi.dat like the
+reference program) reproduces the reference's FP64 run of config 0."""
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from pfdd_gb300 import build, refio, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def test_host_driver_reproduces_reference_run(native_lib, tmp_path):
+    spec, z = load_golden("config0_32c_ns3_k200")
+    xi, bc = workloads.initial_state(spec)
+    refio.write_xi_files(tmp_path, xi, bc, ns_ref=12)
+    r = subprocess.run([str(build.RUNNER), *map(str, spec.n), str(spec.ns), str(spec.steps), repr(spec.sigma_max),
+                        "--nsfile", "12"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    g = np.loadtxt(tmp_path / "gamma_full.dat", ndmin=2)
+    assert g.shape[0] == spec.steps
+    np.testing.assert_allclose(g[:, 1], z["gamma"], rtol=1e-9)
+    lines = (tmp_path / "phasefield.dat").read_text().splitlines()
+    assert len(lines) == spec.steps and lines[0].split()[:2] == ["1", "1"]
+    xf = refio.read_xi_file(tmp_path / "xi.dat", spec.n, 21)
+    flat = xf[:3].reshape(3, -1)
+    assert np.max(np.abs(flat[:, z["sample_idx"]] - z["xi_final_sample"])) <= 1e-10
+    assert np.all(xf[3:] == 0)
+
+
+def test_host_driver_fp32_form(native_lib, tmp_path):
+    spec, z = load_golden("config0_32c_ns3_k200")
+    xi, bc = workloads.initial_state(spec)
+    refio.write_xi_files(tmp_path, xi, bc, ns_ref=12)
+    r = subprocess.run([str(build.RUNNER), *map(str, spec.n), str(spec.ns), str(spec.steps), repr(spec.sigma_max),
+                        "--nsfile", "12", "--fp32"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    g = np.loadtxt(tmp_path / "gamma_full.dat", ndmin=2)
+    np.testing.assert_allclose(g[:, 1], z["gamma"], rtol=1e-5)

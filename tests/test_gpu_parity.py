@@ -1,0 +1,203 @@
+"""CUDA path (through the C ABI) against the CPU FP64 oracle and the reference's golden
+vectors.
+
+Tolerances: plain FP64 form max|dxi| <= 1e-10 and gamma relative error <= 1e-9
+(the plain-form parity bar); FP32-FFT form gamma relative error <= 1e-5 against the
+FP64 oracle."""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from oracle import oracle
+from pfdd_gb300 import native, workloads
+
+pytestmark = pytest.mark.gpu
+
+XI_TOL = 1e-10
+GAMMA_RTOL = 1e-9
+FP32_GAMMA_RTOL = 1e-5
+
+
+def run_gpu(spec, precision="fp64", steps=None, bc=None, xi=None):
+    K = spec.steps if steps is None else steps
+    s = native.solver_for(spec, precision)
+    try:
+        x0, b0 = workloads.initial_state(spec)
+        s.set_state(x0 if xi is None else xi, b0 if bc is None else bc)
+        tau = native.spec_tau(spec)[:K]
+        g, ga = s.step(tau)
+        return s.get_state()[0], g[:, 0], ga[:, 0], s.launches
+    finally:
+        s.close()
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_fp64_matches_reference_golden(native_lib, name):
+    spec, z = load_golden(name)
+    xf, g, ga, launches = run_gpu(spec)
+    assert launches >= spec.steps * 6
+    assert rel(g, z["gamma"]) <= GAMMA_RTOL
+    assert np.max(np.abs(ga - z["gamma_a"])) <= GAMMA_RTOL * max(1e-3, np.max(np.abs(z["gamma_a"])))
+    flat = xf.reshape(spec.ns, -1)
+    if "xi_final" in z:
+        err = np.max(np.abs(flat - z["xi_final"]))
+    else:
+        err = np.max(np.abs(flat[:, z["sample_idx"]] - z["xi_final_sample"]))
+    assert err <= XI_TOL, err
+
+
+def test_fp64_matches_oracle_config0_full_field(native_lib):
+    spec = workloads.config0()
+    xo, go, gao = oracle.solve(spec)
+    xf, g, ga, _ = run_gpu(spec)
+    assert np.max(np.abs(xf - xo)) <= XI_TOL
+    assert rel(g, go) <= GAMMA_RTOL
+    assert np.max(np.abs(xo.imag)) > 1e-4  # Im(xi) really evolves (Nyquist planes)
+
+
+def test_device_B_matches_reference_formula(native_lib):
+    for n in [(8, 16, 4), (32, 32, 32), (2, 8, 1)]:
+        eps = oracle.fcc_eps(12)
+        for C11 in (3.5, 4.2):
+            Bo = oracle.bmatrix(n, eps, C11, 1.5, 1.0)
+            s = native.Solver(n, 12, "fp64")
+            s.build_B(C11, 1.5, 1.0, eps)
+            Bg = s.get_B()
+            s.close()
+            assert np.max(np.abs(Bg - Bo)) <= 1e-13 * max(1.0, np.max(np.abs(Bo)))
+
+
+def test_set_B_host_path_equals_device_build(native_lib):
+    spec = workloads.SolveSpec(n=(16, 8, 16), ns=12, steps=6, sigma_max=0.05,
+                               loops=workloads.random_loops((16, 8, 16), 3, 2.0, 5.0, 12, seed=3), noise_seed=3)
+    eps = oracle.fcc_eps(12)
+    Bo = oracle.bmatrix(spec.n, eps, 3.5, 1.5, 1.0)
+    s = native.Solver(spec.n, 12, "fp64")
+    s.set_B(Bo)
+    s.set_params(0.01, 0.1, 1.0)
+    x0, b0 = workloads.initial_state(spec)
+    s.set_state(x0, b0)
+    g, _ = s.step(native.spec_tau(spec))
+    xs = s.get_state()[0]
+    s.close()
+    xo, go, _ = oracle.solve(spec)
+    assert np.max(np.abs(xs - xo)) <= XI_TOL and rel(g[:, 0], go) <= GAMMA_RTOL
+
+
+def test_pinned_points_and_non_cubic(native_lib):
+    spec = workloads.SolveSpec(n=(16, 4, 32), ns=12, steps=12, sigma_max=0.06,
+                               loops=workloads.random_loops((16, 4, 32), 4, 2.0, 6.0, 12, seed=9), noise_seed=9)
+    x0, bc = workloads.initial_state(spec)
+    rng = np.random.default_rng(1)
+    bc = (rng.random(bc.shape) < 0.2).astype(np.float64) * rng.choice([1.0, 2.0], size=bc.shape)
+    xf, g, _, _ = run_gpu(spec, bc=bc)
+    eps = oracle.fcc_eps(12)
+    B = oracle.bmatrix(spec.n, eps, 3.5, 1.5, 1.0)
+    tau = native.spec_tau(spec)
+    xo, go, _ = oracle.run(spec.n, B, x0, bc, [0.01] * 12, [0.1] * 12, [1.0] * 12, 1.0, tau)
+    assert np.max(np.abs(xf - xo)) <= XI_TOL and rel(g, go) <= GAMMA_RTOL
+    pinned = bc != 0
+    np.testing.assert_array_equal(xf[pinned], x0[pinned])
+
+
+def test_tau_field_mode(native_lib):
+    spec = workloads.SolveSpec(n=(8, 16, 16), ns=3, steps=8, sigma_max=0.0,
+                               loops=[workloads.Loop(1, (4, 8, 8), 4.0)], noise_seed=2)
+    rng = np.random.default_rng(4)
+    tf = rng.uniform(-0.1, 0.1, size=(spec.npts, 3))  # [i][j][k][ns]
+    mult = np.linspace(0.1, 1.0, spec.steps)[:, None] * np.ones((1, 3))
+    s = native.solver_for(spec)
+    x0, b0 = workloads.initial_state(spec)
+    s.set_state(x0, b0)
+    s.set_tau_field(tf)
+    g, _ = s.step(mult)
+    xs = s.get_state()[0]
+    s.close()
+    eps = oracle.fcc_eps(3)
+    B = oracle.bmatrix(spec.n, eps, 3.5, 1.5, 1.0)
+    xo, go, _ = oracle.run(spec.n, B, x0, b0, [0.01] * 3, [0.1] * 3, [1.0] * 3, 1.0, mult, tau_field=tf)
+    assert np.max(np.abs(xs - xo)) <= XI_TOL and rel(g[:, 0], go) <= GAMMA_RTOL
+
+
+def test_step_chunks_and_restart_are_seamless(native_lib):
+    spec = workloads.SolveSpec(n=(16, 16, 16), ns=3, steps=20, sigma_max=0.05,
+                               loops=[workloads.Loop(0, (8, 8, 8), 5.0)], noise_seed=4)
+    xa, ga_, _, _ = run_gpu(spec)
+    s = native.solver_for(spec)
+    x0, b0 = workloads.initial_state(spec)
+    s.set_state(x0, b0)
+    tau = native.spec_tau(spec)
+    g1, _ = s.step(tau[:7])
+    g2, _ = s.step(tau[7:])
+    xb = s.get_state()[0]
+    s.close()
+    np.testing.assert_array_equal(xa, xb)
+    np.testing.assert_array_equal(ga_, np.concatenate([g1[:, 0], g2[:, 0]]))
+
+
+def test_batched_replicas_equal_individual_runs(native_lib):
+    base = workloads.SolveSpec(n=(16, 8, 32), ns=12, steps=10, sigma_max=0.05,
+                               loops=workloads.random_loops((16, 8, 32), 3, 2.0, 5.0, 12, seed=5))
+    specs = []
+    for r, sig in enumerate([0.01, 0.05, 0.08]):
+        sp = workloads.SolveSpec(**{**base.__dict__, "noise_seed": 50 + r, "sigma_max": sig})
+        specs.append(sp)
+    for prec in ("fp64", "fp32"):
+        s = native.solver_for(specs[0], prec, nrep=3)
+        xs = np.stack([workloads.initial_state(sp)[0] for sp in specs])
+        bcs = np.stack([workloads.initial_state(sp)[1] for sp in specs])
+        s.set_state(xs, bcs)
+        tau = np.stack([native.spec_tau(sp) for sp in specs], axis=1)
+        g, ga = s.step(tau)
+        xb = s.get_state()
+        s.close()
+        for r, sp in enumerate(specs):
+            xr, gr, _, _ = run_gpu(sp, prec)
+            np.testing.assert_array_equal(xb[r], xr)
+            np.testing.assert_array_equal(g[:, r], gr)
+
+
+def test_idle_replica_keeps_state(native_lib):
+    spec = workloads.SolveSpec(n=(8, 8, 8), ns=3, steps=5, sigma_max=0.05,
+                               loops=[workloads.Loop(0, (4, 4, 4), 3.0)], noise_seed=1)
+    s = native.solver_for(spec, "fp64", nrep=2)
+    x0, b0 = workloads.initial_state(spec)
+    s.set_state(np.stack([x0, x0]), np.stack([b0, b0]))
+    s.set_active(1, False)
+    s.step(np.stack([native.spec_tau(spec)] * 2, axis=1))
+    xb = s.get_state()
+    s.close()
+    np.testing.assert_array_equal(xb[1], x0)
+    assert np.max(np.abs(xb[0] - x0)) > 0
+
+
+def test_fp32_form_error_vs_fp64_oracle(native_lib):
+    spec = workloads.config0()
+    xo, go, _ = oracle.solve(spec)
+    xf, g, _, _ = run_gpu(spec, "fp32")
+    assert rel(g, go) <= FP32_GAMMA_RTOL
+    assert np.max(np.abs(xf - xo)) <= 1e-5
+
+
+def test_nonfinite_state_is_reported(native_lib):
+    spec = workloads.SolveSpec(n=(8, 8, 8), ns=3, steps=3, sigma_max=0.0, noise_seed=0)
+    s = native.solver_for(spec)
+    x0, b0 = workloads.initial_state(spec)
+    x0[0, 1, 2, 3] = np.nan
+    s.set_state(x0, b0)
+    with pytest.raises(native.PFDDError) as ei:
+        s.step(np.zeros((3, 3)))
+    assert ei.value.status == native.PFDD_ENONFINITE
+    s.close()
+
+
+def test_missing_inputs_are_reported(native_lib):
+    s = native.Solver((8, 8, 8), 3)
+    with pytest.raises(native.PFDDError) as ei:
+        s.step(np.zeros((1, 3)))
+    assert ei.value.status == native.PFDD_ENOTREADY
+    s.close()
