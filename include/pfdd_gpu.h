@@ -123,6 +123,17 @@ pfdd_status pfdd_set_replica_active(pfdd_ctx *ctx, int r, int active);
 /* Number of kernel launches issued by the last pfdd_step call. */
 long long pfdd_last_launch_count(const pfdd_ctx *ctx);
 
+/* The context's CUDA stream (a cudaStream_t), so callers can order their own
+ * work and events against the step. */
+void *pfdd_get_stream(pfdd_ctx *ctx);
+
+/* Measurement: with timing on, every kernel launch of the context is bracketed
+ * by a CUDA event pair on the context's stream.  pfdd_kernel_stat reports, for
+ * kernel kind idx (0 .. until it returns PFDD_EINVAL), its name, the number of
+ * timed launches and their total device time since timing was (re)enabled. */
+pfdd_status pfdd_set_kernel_timing(pfdd_ctx *ctx, int enable);
+pfdd_status pfdd_kernel_stat(pfdd_ctx *ctx, int idx, const char **name, long long *launches, double *total_ms);
+
 /* Device bytes held by a context of this shape (admission control). */
 size_t pfdd_required_bytes(int n1, int n2, int n3, int ns, int nrep, int precision);
 

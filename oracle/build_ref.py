@@ -22,7 +22,8 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
 2   4315, 1903                 ``setfcc`` instead of ``set3D1sys``; Burgers vector
                                scaled by ``PFDD_BDIV`` (sqrt(2) gives |b|=1)
 3   4186                       ``choice=2``: read xi.dat / xi_bc.dat
-4   4205                       ``plastic_max = PFDD_K`` (fixed step count)
+4   4205                       ``plastic_max = PFDD_K`` (fixed step count; the
+                               environment variable PFDD_KRUN may run fewer)
 5   4580                       ``interfacevolv`` disabled (bimaterial special case)
 6   1432                       regression fix: the virtual DD term is not added to
                                slip row ``isb`` (the older program's semantics)
@@ -88,6 +89,7 @@ DEFAULTS_BLOCK = r"""
 #ifndef PFDD_SETUP_B
 #define PFDD_SETUP_B 1
 #endif
+static int pfdd_krun_(int k_) { const char *s_ = getenv("PFDD_KRUN"); return s_ ? atoi(s_) : k_; }
 #define PFDD_LOG_STEP(itp_, g_, g1_) do { static FILE *pfdd_gf_; int q_; \
     if (!pfdd_gf_) pfdd_gf_ = fopen("gamma_full.dat", "w"); \
     fprintf(pfdd_gf_, "%d %.17e", (itp_), (double)(g_)); \
@@ -124,7 +126,7 @@ PATCHES = [
     (4162, "GG = malloc((2*(NS)*(NS)*(N1)*(N2)*(N3))*sizeof(double));",
      "GG = calloc((size_t)(2*(NS)*(NS)*(N1)*(N2)*(N3)), sizeof(double));"),
     (4186, "choice=1;", "choice=2;"),
-    (4205, "plastic_max =3000;", "plastic_max =PFDD_K;"),
+    (4205, "plastic_max =3000;", "plastic_max =pfdd_krun_(PFDD_K);"),
     (4278, "Asf2[is] = 0.0262;", "Asf2[is] = PFDD_ASF;"),
     (4280, "Asf2[0] = 0.0064659518668288441;", "Asf2[0] = PFDD_ASF;"),
     (4281, "Asf2[1] = 0.0064659518668288441;", "Asf2[1] = PFDD_ASF;"),

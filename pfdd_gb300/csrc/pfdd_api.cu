@@ -73,6 +73,22 @@ cudaError_t set_smem_attrs(size_t maxsmem) {
   return cudaFuncSetAttribute(fft_strided_kernel<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
 }
 
+// kernels of a step, for the optional per-kernel event timing
+enum KId { K_Z_PROLOGUE, K_Z_STEP, K_FFT_Y_FWD, K_FFT_X_FWD, K_CONTRACT, K_FFT_X_INV, K_FFT_Y_INV, K_GAMMA,
+           K_X_FUSED, K_PLANE, K_PLANE_PROLOGUE, K_COUNT };
+const char *const kKernelNames[K_COUNT] = {"z_prologue", "z_step", "fft_y_fwd", "fft_x_fwd", "contract",
+                                           "fft_x_inv", "fft_y_inv", "gamma_reduce", "x_fused", "plane",
+                                           "plane_prologue"};
+
+struct KTiming {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<int> ids;
+  size_t used = 0;
+  double ms[K_COUNT] = {};
+  long long cnt[K_COUNT] = {};
+};
+
 }  // namespace
 
 struct pfdd_ctx {
@@ -87,6 +103,7 @@ struct pfdd_ctx {
   double *tau = nullptr, *part = nullptr, *gam_a = nullptr, *gam = nullptr;
   double *tau_field = nullptr, *dslip_dev = nullptr;
   uint8_t *active = nullptr;
+  int *flag = nullptr;
   void *tw[3] = {nullptr, nullptr, nullptr};
   double *h_gam_a = nullptr, *h_gam = nullptr, *h_tau = nullptr;
   std::vector<uint8_t> h_active;
@@ -95,6 +112,7 @@ struct pfdd_ctx {
   int kchunk = 1;
   Geometry g;
   long long launches = 0;
+  KTiming tm;
   std::string err;
 };
 
@@ -128,6 +146,24 @@ static pfdd_status fail(pfdd_ctx *c, pfdd_status s, const char *fmt, ...) {
                   #call, cudaGetErrorString(e_), __FILE__, __LINE__);                          \
     }                                                                                         \
   } while (0)
+
+// CUDA event pair around one kernel launch (timing mode only)
+static void t_begin(pfdd_ctx *c) {
+  if (!c->tm.on) return;
+  while (c->tm.pool.size() < c->tm.used + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) { c->tm.on = false; return; }
+    c->tm.pool.push_back(e);
+  }
+  cudaEventRecord(c->tm.pool[c->tm.used], c->st);
+}
+static void t_end(pfdd_ctx *c, int id) {
+  c->launches++;
+  if (!c->tm.on) return;
+  cudaEventRecord(c->tm.pool[c->tm.used + 1], c->st);
+  c->tm.ids.push_back(id);
+  c->tm.used += 2;
+}
 
 static size_t vsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double2) : sizeof(float2); }
 static size_t bsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double) : sizeof(float); }
@@ -194,6 +230,7 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   CK(c, cudaMalloc(&c->B, P * N * bsize_of(precision)));
   CK(c, cudaMalloc(&c->active, nrep));
   CK(c, cudaMalloc(&c->dslip_dev, kMaxNs * sizeof(double)));
+  CK(c, cudaMalloc(&c->flag, sizeof(int)));
   // partial sums for a chunk of steps, bounded to ~32 MB
   const size_t per_step = RF * (size_t)c->g.zNparts;
   c->kchunk = (int)std::max<size_t>(1, std::min<size_t>(1024, (4u << 20) / std::max<size_t>(per_step, 1)));
@@ -220,7 +257,8 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   cudaSetDevice(c->dev);
   if (c->st) cudaStreamSynchronize(c->st);
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
-                c->active, c->tw[0], c->tw[1], c->tw[2]};
+                c->active, c->flag, c->tw[0], c->tw[1], c->tw[2]};
+  for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
   for (void *p : dp)
     if (p) cudaFree(p);
   if (c->h_gam_a) cudaFreeHost(c->h_gam_a);
@@ -329,35 +367,40 @@ extern "C" pfdd_status pfdd_set_params(pfdd_ctx *c, const double *cd2, const dou
   return PFDD_OK;
 }
 
-// Upload xi (and the pinned mask) of replicas [r0, r0+nr).
+// Upload xi (and the pinned mask) of replicas [r0, r0+nr).  xi_bc is staged
+// through the spectral buffer S (invalidated by a state change anyway) in
+// chunks and packed to bits on the device, so no host pass over it is needed.
 static pfdd_status upload_state(pfdd_ctx *c, int r0, int nr, const double *xi, const double *bc) {
   CK(c, cudaSetDevice(c->dev));
   const size_t fieldN = (size_t)c->N, RFn = (size_t)nr * c->ns;
   CK(c, cudaMemcpyAsync(c->xi + (size_t)r0 * c->ns * fieldN, xi, RFn * fieldN * sizeof(double2),
                         cudaMemcpyHostToDevice, c->st));
-  // pinned mask: bit set where xi_bc[..][0] != 0 (the reference tests == 0 to evolve, F:3481)
-  bool any = false;
-  if (bc)
-    for (size_t e = 0; e < RFn * fieldN && !any; ++e) any = bc[2 * e] != 0.0;
   const size_t total_bits = (size_t)c->nrep * c->ns * fieldN, words = (total_bits + 31) / 32;
-  if (any && !c->bc) {
+  if (bc && !c->bc) {
     CK(c, cudaMalloc(&c->bc, words * 4));
     CK(c, cudaMemsetAsync(c->bc, 0, words * 4, c->st));
   }
   if (c->bc) {
-    // rebuild the words of this replica range on the host (range is word-aligned only
-    // when ns*N is a multiple of 32, so read-modify-write the whole mask)
-    std::vector<uint32_t> m(words);
-    CK(c, cudaMemcpyAsync(m.data(), c->bc, words * 4, cudaMemcpyDeviceToHost, c->st));
-    CK(c, cudaStreamSynchronize(c->st));
-    const size_t b0 = (size_t)r0 * c->ns * fieldN;
-    for (size_t e = 0; e < RFn * fieldN; ++e) {
-      const size_t bit = b0 + e;
-      const bool pin = bc && bc[2 * e] != 0.0;
-      if (pin) m[bit >> 5] |= (1u << (bit & 31));
-      else m[bit >> 5] &= ~(1u << (bit & 31));
+    const size_t count = RFn * fieldN, b0 = (size_t)r0 * c->ns * fieldN;
+    if (!bc) {
+      // every point of these replicas evolves: clear their bits
+      CK(c, cudaMemsetAsync(c->S, 0, std::min(count, (size_t)c->nrep * c->ns * fieldN * vsize_of(c->prec) / 16) * 16,
+                            c->st));
     }
-    CK(c, cudaMemcpyAsync(c->bc, m.data(), words * 4, cudaMemcpyHostToDevice, c->st));
+    const size_t chunk = (size_t)c->nrep * c->ns * fieldN * vsize_of(c->prec) / (2 * sizeof(double));
+    for (size_t off = 0; off < count; off += chunk) {
+      const size_t n = std::min(chunk, count - off);
+      if (bc) CK(c, cudaMemcpyAsync(c->S, bc + 2 * off, n * 2 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+      pack_bc_kernel<<<1216, kThreads, 0, c->st>>>((const double *)c->S, (long long)n, (long long)(b0 + off), c->bc);
+      CK(c, cudaGetLastError());
+    }
+    CK(c, cudaMemsetAsync(c->flag, 0, sizeof(int), c->st));
+    mask_any_kernel<<<304, kThreads, 0, c->st>>>(c->bc, (long long)words, c->flag);
+    CK(c, cudaGetLastError());
+    int any = 0;
+    CK(c, cudaMemcpyAsync(&any, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaStreamSynchronize(c->st));
+    c->anyBc = any != 0;
   }
   CK(c, cudaStreamSynchronize(c->st));
   c->hasState = true;
@@ -406,8 +449,9 @@ template <typename T>
 static cudaError_t launch_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
   const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
+  t_begin(c);
   zpass_kernel<T><<<(unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st>>>(zp);
-  c->launches++;
+  t_end(c, (flags & Z_UPDATE) ? K_Z_STEP : K_Z_PROLOGUE);
   return cudaGetLastError();
 }
 
@@ -420,9 +464,10 @@ static cudaError_t launch_strided(pfdd_ctx *c, int ax /*0: y, 1: x*/) {
   const long long outer = ax == 0 ? (long long)c->nrep * c->ns * c->n[0] : (long long)c->nrep * c->ns;
   const long long outer_per_rep = outer / c->nrep;
   const long long blocks = outer * c->g.tiles[gi];
+  t_begin(c);
   fft_strided_kernel<T, S><<<(unsigned)blocks, c->g.threads[gi], c->g.smem[gi], c->st>>>(
       c->S, L, inner, c->g.TI[gi], c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0], c->active, outer_per_rep, c->g.pitch[gi]);
-  c->launches++;
+  t_end(c, ax == 0 ? (S < 0 ? K_FFT_Y_FWD : K_FFT_Y_INV) : (S < 0 ? K_FFT_X_FWD : K_FFT_X_INV));
   return cudaGetLastError();
 }
 
@@ -432,11 +477,12 @@ static cudaError_t launch_contract_ns(pfdd_ctx *c) {
   // FP32 batches: 2-4 replicas per pass reuse each loaded B value (register budget
   // allows 4 for NS <= 4, 2 up to NS = 12); FP64 keeps one replica per pass.
   constexpr int RCF = std::is_same<T, float>::value ? (NS <= 4 ? 4 : 2) : 1;
+  t_begin(c);
   if (RCF > 1 && c->nrep > 1)
     contract_kernel<T, NS, RCF><<<blocks, kThreads, 0, c->st>>>(c->S, (const T *)c->B, c->N, c->nrep, c->active);
   else
     contract_kernel<T, NS, 1><<<blocks, kThreads, 0, c->st>>>(c->S, (const T *)c->B, c->N, c->nrep, c->active);
-  c->launches++;
+  t_end(c, K_CONTRACT);
   return cudaGetLastError();
 }
 
@@ -463,7 +509,7 @@ template <typename T>
 static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double *gamma, double *gamma_a) {
   ZParams zp;
   std::memset(&zp, 0, sizeof zp);
-  zp.S = c->S; zp.xi = c->xi; zp.bc = c->bc; zp.tau = c->tau; zp.tau_field = c->tau_field;
+  zp.S = c->S; zp.xi = c->xi; zp.bc = c->anyBc ? c->bc : nullptr; zp.tau = c->tau; zp.tau_field = c->tau_field;
   zp.dslip = c->dslip_dev; zp.part = c->part;
   zp.active = c->active;
   zp.tw = c->tw[2];
@@ -502,9 +548,10 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
       CK(c, launch_zpass<T>(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE));
     }
     const int nt = ks * c->nrep;
+    t_begin(c);
     gamma_reduce_kernel<<<(nt + 127) / 128, 128, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, ks, zp.inv_n,
                                                              c->gam_a, c->gam);
-    c->launches++;
+    t_end(c, K_GAMMA);
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(c->h_gam_a, c->gam_a, (size_t)ks * RF * sizeof(double), cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaMemcpyAsync(c->h_gam, c->gam, (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -545,6 +592,37 @@ extern "C" pfdd_status pfdd_get_replica_state(pfdd_ctx *c, int r, double *xi) {
   const size_t fl = (size_t)c->ns * c->N;
   CK(c, cudaMemcpyAsync(xi, c->xi + (size_t)r * fl, fl * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
   CK(c, cudaStreamSynchronize(c->st));
+  return PFDD_OK;
+}
+
+extern "C" void *pfdd_get_stream(pfdd_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+extern "C" pfdd_status pfdd_set_kernel_timing(pfdd_ctx *c, int enable) {
+  if (!c) return PFDD_EINVAL;
+  c->tm.on = enable != 0;
+  c->tm.used = 0;
+  c->tm.ids.clear();
+  for (int k = 0; k < K_COUNT; ++k) { c->tm.ms[k] = 0; c->tm.cnt[k] = 0; }
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_kernel_stat(pfdd_ctx *c, int idx, const char **name, long long *launches,
+                                        double *total_ms) {
+  if (!c || idx < 0 || idx >= K_COUNT) return PFDD_EINVAL;
+  if (c->tm.used) {  // fold recorded event pairs into the totals
+    CK(c, cudaStreamSynchronize(c->st));
+    for (size_t q = 0; q < c->tm.ids.size(); ++q) {
+      float ms = 0.f;
+      CK(c, cudaEventElapsedTime(&ms, c->tm.pool[2 * q], c->tm.pool[2 * q + 1]));
+      c->tm.ms[c->tm.ids[q]] += ms;
+      c->tm.cnt[c->tm.ids[q]] += 1;
+    }
+    c->tm.used = 0;
+    c->tm.ids.clear();
+  }
+  if (name) *name = kKernelNames[idx];
+  if (launches) *launches = c->tm.cnt[idx];
+  if (total_ms) *total_ms = c->tm.ms[idx];
   return PFDD_OK;
 }
 

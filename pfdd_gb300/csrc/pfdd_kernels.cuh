@@ -335,6 +335,40 @@ __global__ void pack_B_kernel(const double *src, int ns, long long N, double *Bd
   }
 }
 
+// xi_bc -> pinned bit mask (bit set where xi_bc[..][0] != 0; the reference
+// evolves a point where XI_BC(...,0) == 0, F:3481).  `src` holds count
+// interleaved [re, im] pairs for bits bit0 .. bit0+count-1; each warp builds its
+// 32 bits with a ballot and merges them into at most two mask words.
+__global__ void pack_bc_kernel(const double *src, long long count, long long bit0, uint32_t *mask) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31LL; base < count; base += stride) {
+    const long long e = base + (threadIdx.x & 31);
+    const bool pin = e < count && src[2 * e] != 0.0;
+    const uint32_t bal = __ballot_sync(0xffffffffu, pin);
+    if ((threadIdx.x & 31) == 0) {
+      const long long n = count - base < 32 ? count - base : 32;
+      const long long b = bit0 + base;
+      const int sh = (int)(b & 31);
+      const unsigned long long m64 = (n == 32 ? 0xffffffffull : ((1ull << n) - 1)) << sh;
+      const unsigned long long p64 = ((unsigned long long)bal & (n == 32 ? 0xffffffffull : ((1ull << n) - 1))) << sh;
+      uint32_t *w = mask + (b >> 5);
+      atomicAnd(w, ~(uint32_t)m64);
+      atomicOr(w, (uint32_t)p64);
+      if (m64 >> 32) {
+        atomicAnd(w + 1, ~(uint32_t)(m64 >> 32));
+        atomicOr(w + 1, (uint32_t)(p64 >> 32));
+      }
+    }
+  }
+}
+
+__global__ void mask_any_kernel(const uint32_t *mask, long long words, int *any) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int found = 0;
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += stride) found |= mask[w] != 0u;
+  if (__syncthreads_or(found) && threadIdx.x == 0) atomicOr(any, 1);
+}
+
 // Inverse of pack_B_kernel: pair layout (FP64 or FP32) -> [kb][ka][N] FP64.
 __global__ void unpack_B_kernel(const double *Bd, const float *Bf, int ns, long long N, double *dst) {
   const long long stride = (long long)gridDim.x * blockDim.x;

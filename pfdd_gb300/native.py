@@ -29,7 +29,7 @@ EXPORTS = [
     "pfdd_get_state", "pfdd_get_replica_state", "pfdd_set_replica_active", "pfdd_last_launch_count",
     "pfdd_required_bytes", "pfdd_fft_plan_create", "pfdd_fft_plan_destroy", "pfdd_fft_forward",
     "pfdd_fft_backward", "pfdd_status_string", "pfdd_frec", "pfdd_setfcc", "pfdd_setorient", "pfdd_seteps",
-    "pfdd_resolve_shear", "pfdd_ramp_tau",
+    "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
 ]
 
 _lib = None
@@ -70,6 +70,10 @@ def load():
     L.pfdd_set_replica_active.argtypes = [vp, i, i]
     L.pfdd_last_launch_count.argtypes = [vp]
     L.pfdd_last_launch_count.restype = C.c_longlong
+    L.pfdd_get_stream.argtypes = [vp]
+    L.pfdd_get_stream.restype = vp
+    L.pfdd_set_kernel_timing.argtypes = [vp, i]
+    L.pfdd_kernel_stat.argtypes = [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     L.pfdd_required_bytes.argtypes = [i, i, i, i, i, i]
     L.pfdd_required_bytes.restype = sz
     L.pfdd_fft_plan_create.argtypes = [C.POINTER(vp), i, i, i, i, i, i]
@@ -236,6 +240,28 @@ class Solver:
     @property
     def launches(self) -> int:
         return int(self.L.pfdd_last_launch_count(self.h))
+
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(self.L.pfdd_get_stream(self.h) or 0)
+
+    def kernel_timing(self, on: bool):
+        self._check(self.L.pfdd_set_kernel_timing(self.h, int(bool(on))), "pfdd_set_kernel_timing")
+
+    def kernel_stats(self) -> dict:
+        """{kernel name: (timed launches, total device ms)} since timing was enabled."""
+        out = {}
+        idx = 0
+        while True:
+            nm = C.c_char_p(); cnt = C.c_longlong(); ms = C.c_double()
+            st = self.L.pfdd_kernel_stat(self.h, idx, C.byref(nm), C.byref(cnt), C.byref(ms))
+            if st != PFDD_OK:
+                break
+            if cnt.value:
+                out[nm.value.decode()] = (int(cnt.value), float(ms.value))
+            idx += 1
+        return out
 
 
 class FFTPlan:
