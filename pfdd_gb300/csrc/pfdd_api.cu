@@ -18,7 +18,144 @@
 #include <vector>
 
 #include "../../include/pfdd_gpu.h"
-#include "pfdd_kernels.cuh"
+#include "pfdd_launch.h"
+
+namespace pfdd {
+
+// Deterministic second stage of the gamma sums: one block per (step, replica),
+// fixed-shape tree over the partials of each system.
+__global__ void __launch_bounds__(256) gamma_reduce_kernel(const double *part, int nparts, int R, int ns,
+                                                           double inv_n, double *gamma_a, double *gamma) {
+  __shared__ double red[32];
+  const int s = blockIdx.x / R, r = blockIdx.x - s * R;
+  double tot = 0.0;
+  for (int a = 0; a < ns; ++a) {
+    const double *pp = part + ((long long)s * R * ns + (long long)r * ns + a) * nparts;
+    double acc = 0.0;
+    for (int c = threadIdx.x; c < nparts; c += blockDim.x) acc += pp[c];
+    const double sum = block_sum(acc, red);
+    if (threadIdx.x == 0) {
+      gamma_a[((long long)s * R + r) * ns + a] = sum * inv_n;
+      tot += sum;
+    }
+  }
+  if (threadIdx.x == 0) gamma[blockIdx.x] = tot * inv_n;
+}
+
+// B(k) of Bmatrix (F:328-412) in closed form:
+//   B_ab = (E_ab - t_a^T G t_b) / mu,  t_a = sigma_a f,
+//   G_ki = (1/f^2) [delta_ik / (mu + mu' z_k)
+//                   - f_i f_k / f^2 / (mu + mu' z_i) / (mu + mu' z_k) (mu + lambda) / kk]
+// with z_i = f_i^2 / f^2 and kk = 1 + (mu + lambda) sum_j z_j / (mu + mu' z_j).
+__global__ void build_B_kernel(const BBuildParams *__restrict__ bp, BLayout bl, double *Bd, float *Bf) {
+  const long long N = bl.N;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int ns = bp->ns;
+  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
+    const int k3 = (int)(pt % bp->n3), k2 = (int)((pt / bp->n3) % bp->n2), k1 = (int)(pt / ((long long)bp->n3 * bp->n2));
+    const double f[3] = {frec_dev(k1, bp->n1, bp->d1), frec_dev(k2, bp->n2, bp->d2), frec_dev(k3, bp->n3, bp->d3)};
+    const double f2 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    if (!(f2 > 0)) {
+      for (int q = 0; q < bl.P; ++q) {
+        const long long bi = b_index(bl, q, pt);
+        if (Bd) Bd[bi] = 0.0;
+        if (Bf) Bf[bi] = 0.0f;
+      }
+      continue;
+    }
+    const double mu = bp->mu, ll = bp->ll, mup = bp->mup;
+    double z[3], den[3];
+    for (int i = 0; i < 3; ++i) { z[i] = f[i] * f[i] / f2; den[i] = mu + mup * z[i]; }
+    const double kk = 1.0 + (mu + ll) * (1 / den[0] * z[0] + 1 / den[1] * z[1] + 1 / den[2] * z[2]);
+    double G[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k)
+        G[i][k] = 1 / f2 * ((i == k ? 1.0 : 0.0) / den[k] - f[i] * f[k] / f2 / den[i] / den[k] * (mu + ll) / kk);
+    double t[kMaxNs][3], u[kMaxNs][3];
+    for (int a = 0; a < ns; ++a) {
+      for (int i = 0; i < 3; ++i)
+        t[a][i] = bp->sig[a][i][0] * f[0] + bp->sig[a][i][1] * f[1] + bp->sig[a][i][2] * f[2];
+      for (int i = 0; i < 3; ++i) u[a][i] = G[i][0] * t[a][0] + G[i][1] * t[a][1] + G[i][2] * t[a][2];
+    }
+    int q = 0;
+    for (int a = 0; a < ns; ++a)
+      for (int b = a; b < ns; ++b, ++q) {
+        const double v = (bp->E[a][b] - (t[a][0] * u[b][0] + t[a][1] * u[b][1] + t[a][2] * u[b][2])) * bp->mu_inv;
+        const long long bi = b_index(bl, q, pt);
+        if (Bd) Bd[bi] = v;
+        if (Bf) Bf[bi] = (float)v;
+      }
+  }
+}
+
+// Host-layout B ([kb][ka][N], FP64, on the device) -> device layout.
+__global__ void pack_B_kernel(const double *src, int ns, BLayout bl, double *Bd, float *Bf) {
+  const long long N = bl.N;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
+    int q = 0;
+    for (int a = 0; a < ns; ++a)
+      for (int b = a; b < ns; ++b, ++q) {
+        const double v = src[((long long)b * ns + a) * N + pt];
+        const long long bi = b_index(bl, q, pt);
+        if (Bd) Bd[bi] = v;
+        if (Bf) Bf[bi] = (float)v;
+      }
+  }
+}
+
+// Device layout (FP64 or FP32) -> [kb][ka][N] FP64.
+__global__ void unpack_B_kernel(const double *Bd, const float *Bf, int ns, BLayout bl, double *dst) {
+  const long long N = bl.N;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
+    int q = 0;
+    for (int a = 0; a < ns; ++a)
+      for (int b = a; b < ns; ++b, ++q) {
+        const long long bi = b_index(bl, q, pt);
+        const double v = Bd ? Bd[bi] : (double)Bf[bi];
+        dst[((long long)b * ns + a) * N + pt] = v;
+        dst[((long long)a * ns + b) * N + pt] = v;
+      }
+  }
+}
+
+// xi_bc -> pinned bit mask (bit set where xi_bc[..][0] != 0; the reference
+// evolves a point where XI_BC(...,0) == 0, F:3481).  `src` holds count
+// interleaved [re, im] pairs for bits bit0 .. bit0+count-1; each warp builds its
+// 32 bits with a ballot and merges them into at most two mask words.
+__global__ void pack_bc_kernel(const double *src, long long count, long long bit0, uint32_t *mask) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31LL; base < count; base += stride) {
+    const long long e = base + (threadIdx.x & 31);
+    const bool pin = e < count && src[2 * e] != 0.0;
+    const uint32_t bal = __ballot_sync(0xffffffffu, pin);
+    if ((threadIdx.x & 31) == 0) {
+      const long long n = count - base < 32 ? count - base : 32;
+      const long long b = bit0 + base;
+      const int sh = (int)(b & 31);
+      const unsigned long long lowmask = n == 32 ? 0xffffffffull : ((1ull << n) - 1);
+      const unsigned long long m64 = lowmask << sh;
+      const unsigned long long p64 = ((unsigned long long)bal & lowmask) << sh;
+      uint32_t *w = mask + (b >> 5);
+      atomicAnd(w, ~(uint32_t)m64);
+      atomicOr(w, (uint32_t)p64);
+      if (m64 >> 32) {
+        atomicAnd(w + 1, ~(uint32_t)(m64 >> 32));
+        atomicOr(w + 1, (uint32_t)(p64 >> 32));
+      }
+    }
+  }
+}
+
+__global__ void mask_any_kernel(const uint32_t *mask, long long words, int *any) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int found = 0;
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += stride) found |= mask[w] != 0u;
+  if (__syncthreads_or(found) && threadIdx.x == 0) atomicOr(any, 1);
+}
+
+}  // namespace pfdd
 
 using namespace pfdd;
 
@@ -28,17 +165,30 @@ constexpr int kThreads = 256;
 
 bool pow2_ok(int n) { return n >= 1 && n <= 512 && (n & (n - 1)) == 0; }
 
+int ilog2(long long v) {
+  int l = 0;
+  while ((1LL << l) < v) ++l;
+  return l;
+}
+
 struct Geometry {
   // z-pass
-  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1;
+  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0;
   size_t zSmem = 0;
-  // strided passes (y: axis 1, x: axis 0)
-  int TI[2] = {1, 1}, threads[2] = {1, 1}, pitch[2] = {1, 1};
+  // strided passes (y: axis 1, x: axis 0; x only in the FFT-boundary plans)
+  int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1};
   long long tiles[2] = {1, 1};
   size_t smem[2] = {0, 0};
+  // fused x-pass
+  int xLgT = 0, xPitch = 1, xThreads = 256;
+  long long xTiles = 1;
+  size_t xSmem = 0;
 };
 
-Geometry make_geometry(int n1, int n2, int n3, size_t vsize) {
+static int line_pitch(int L) { return L >= 8 ? L + L / 8 : L; }  // pad8 layout of a contiguous line
+
+// ns = 0: no fused x-pass (FFT-boundary plans).  bsize: bytes of a B(k) value.
+Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize) {
   Geometry g;
   const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
   const long long lines = (long long)n1 * n2;
@@ -46,32 +196,45 @@ Geometry make_geometry(int n1, int n2, int n3, size_t vsize) {
   while ((long long)TL > lines) TL >>= 1;
   g.zTL = TL;
   g.zThreads = TL * team3;
-  g.zPitch = L3 >= 8 ? L3 + 1 : L3;
+  g.zPitch = line_pitch(L3);
   g.zNparts = (int)(lines / TL);
-  g.zSmem = (size_t)TL * g.zPitch * vsize;
+  // twiddles + padded S lines (16-byte aligned) + FP64 xi tile
+  g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
+  g.lgL3 = ilog2(L3);
   const int Ls[2] = {n2, n1};
   const long long inner[2] = {(long long)n3, (long long)n2 * n3};
   for (int ax = 0; ax < 2; ++ax) {
     const int L = Ls[ax], E = std::min(8, L), team = L / E;
     int TI = std::max(1, kThreads / team);
     while ((long long)TI > inner[ax]) TI >>= 1;
-    g.TI[ax] = TI;
+    g.lgTI[ax] = ilog2(TI);
     g.threads[ax] = TI * team;
     g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
     g.tiles[ax] = inner[ax] / TI;
-    g.smem[ax] = (size_t)L * g.pitch[ax] * vsize;
+    g.smem[ax] = ((size_t)L + (size_t)L * g.pitch[ax]) * vsize;
+  }
+  if (ns > 0) {
+    // x-pass tile: T consecutive inner indices of all N1 x and all ns fields plus
+    // the tile's B(k), sized for two CTAs per SM (<= 110 KB), T <= 32
+    const long long innerx = (long long)n2 * n3;
+    g.xPitch = line_pitch(n1);
+    int lgT = 5;
+    while (lgT > 0 && ((1LL << lgT) > innerx ||
+                       x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize) > 110 * 1024))
+      --lgT;
+    g.xLgT = lgT;
+    g.xTiles = innerx >> lgT;
+    g.xSmem = x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize);
+    const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
+    const int unit = std::max(32, team);
+    const int cap = vsize == sizeof(double2) ? 256 : 384;  // x_fused_kernel launch bounds
+    int thr = std::min(cap, std::max(npt, lines * team));
+    thr = (thr + unit - 1) / unit * unit;
+    g.xThreads = std::min(thr, cap / unit * unit);
   }
   return g;
 }
 
-template <typename T>
-cudaError_t set_smem_attrs(size_t maxsmem) {
-  cudaError_t e = cudaFuncSetAttribute(zpass_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(fft_strided_kernel<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(fft_strided_kernel<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-}
 
 // kernels of a step, for the optional per-kernel event timing
 enum KId { K_Z_PROLOGUE, K_Z_STEP, K_FFT_Y_FWD, K_FFT_X_FWD, K_CONTRACT, K_FFT_X_INV, K_FFT_Y_INV, K_GAMMA,
@@ -111,6 +274,7 @@ struct pfdd_ctx {
   double cd2[kMaxNs] = {}, asf[kMaxNs] = {}, dslip[kMaxNs] = {}, uq2 = 1.0;
   int kchunk = 1;
   Geometry g;
+  BLayout bl{};
   long long launches = 0;
   KTiming tm;
   std::string err;
@@ -220,10 +384,8 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   c->N = (long long)n1 * n2 * n3;
   CK(c, cudaSetDevice(device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-  c->g = make_geometry(n1, n2, n3, vsize_of(precision));
-  const size_t maxsmem = std::max({c->g.zSmem, c->g.smem[0], c->g.smem[1]});
-  if (precision == PFDD_FP64) CK(c, set_smem_attrs<double>(maxsmem));
-  else CK(c, set_smem_attrs<float>(maxsmem));
+  c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision));
+  c->bl = BLayout{c->N, (long long)n2 * n3, n1, c->g.xLgT, ns * (ns + 1) / 2};
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
   CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
   CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
@@ -276,7 +438,7 @@ extern "C" pfdd_status pfdd_set_B(pfdd_ctx *c, const double *B) {
   CK(c, cudaMalloc(&tmp, full));
   cudaError_t e = cudaMemcpyAsync(tmp, B, full, cudaMemcpyHostToDevice, c->st);
   if (e == cudaSuccess) {
-    pack_B_kernel<<<1216, kThreads, 0, c->st>>>(tmp, c->ns, c->N, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
+    pack_B_kernel<<<1216, kThreads, 0, c->st>>>(tmp, c->ns, c->bl, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
                                                  c->prec == PFDD_FP64 ? nullptr : (float *)c->B);
     e = cudaGetLastError();
   }
@@ -295,7 +457,7 @@ extern "C" pfdd_status pfdd_get_B(pfdd_ctx *c, double *B) {
   double *tmp = nullptr;
   CK(c, cudaMalloc(&tmp, full));
   unpack_B_kernel<<<1216, kThreads, 0, c->st>>>(c->prec == PFDD_FP64 ? (const double *)c->B : nullptr,
-                                                c->prec == PFDD_FP64 ? nullptr : (const float *)c->B, c->ns, c->N, tmp);
+                                                c->prec == PFDD_FP64 ? nullptr : (const float *)c->B, c->ns, c->bl, tmp);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(B, tmp, full, cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -341,8 +503,8 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
   CK(c, cudaMalloc(&dp, sizeof hp));
   cudaError_t e = cudaMemcpyAsync(dp, &hp, sizeof hp, cudaMemcpyHostToDevice, c->st);
   if (e == cudaSuccess) {
-    build_B_kernel<<<1216, 128, 0, c->st>>>(dp, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
-                                            c->prec == PFDD_FP64 ? nullptr : (float *)c->B, c->N);
+    build_B_kernel<<<1216, 128, 0, c->st>>>(dp, c->bl, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
+                                            c->prec == PFDD_FP64 ? nullptr : (float *)c->B);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -445,18 +607,18 @@ extern "C" pfdd_status pfdd_set_replica_active(pfdd_ctx *c, int r, int on) {
   return PFDD_OK;
 }
 
-template <typename T>
-static cudaError_t launch_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
+static int prec_code(int prec) { return prec == PFDD_FP64 ? 0 : 1; }
+
+static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
   const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
   t_begin(c);
-  zpass_kernel<T><<<(unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st>>>(zp);
+  cudaError_t e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp);
   t_end(c, (flags & Z_UPDATE) ? K_Z_STEP : K_Z_PROLOGUE);
-  return cudaGetLastError();
+  return e;
 }
 
-template <typename T, int S>
-static cudaError_t launch_strided(pfdd_ctx *c, int ax /*0: y, 1: x*/) {
+static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/) {
   const int L = ax == 0 ? c->n[1] : c->n[0];
   if (L == 1) return cudaSuccess;
   const int gi = ax == 0 ? 0 : 1;
@@ -465,44 +627,26 @@ static cudaError_t launch_strided(pfdd_ctx *c, int ax /*0: y, 1: x*/) {
   const long long outer_per_rep = outer / c->nrep;
   const long long blocks = outer * c->g.tiles[gi];
   t_begin(c);
-  fft_strided_kernel<T, S><<<(unsigned)blocks, c->g.threads[gi], c->g.smem[gi], c->st>>>(
-      c->S, L, inner, c->g.TI[gi], c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0], c->active, outer_per_rep, c->g.pitch[gi]);
-  t_end(c, ax == 0 ? (S < 0 ? K_FFT_Y_FWD : K_FFT_Y_INV) : (S < 0 ? K_FFT_X_FWD : K_FFT_X_INV));
-  return cudaGetLastError();
-}
-
-template <typename T, int NS>
-static cudaError_t launch_contract_ns(pfdd_ctx *c) {
-  const int blocks = (int)std::min<long long>((c->N + kThreads - 1) / kThreads, 152LL * 8);
-  // FP32 batches: 2-4 replicas per pass reuse each loaded B value (register budget
-  // allows 4 for NS <= 4, 2 up to NS = 12); FP64 keeps one replica per pass.
-  constexpr int RCF = std::is_same<T, float>::value ? (NS <= 4 ? 4 : 2) : 1;
-  t_begin(c);
-  if (RCF > 1 && c->nrep > 1)
-    contract_kernel<T, NS, RCF><<<blocks, kThreads, 0, c->st>>>(c->S, (const T *)c->B, c->N, c->nrep, c->active);
-  else
-    contract_kernel<T, NS, 1><<<blocks, kThreads, 0, c->st>>>(c->S, (const T *)c->B, c->N, c->nrep, c->active);
-  t_end(c, K_CONTRACT);
-  return cudaGetLastError();
+  cudaError_t e = launch_strided(prec_code(c->prec), sign, ilog2(L), (unsigned)blocks, c->g.threads[gi], c->g.smem[gi],
+                                 c->st, c->S, c->g.lgTI[gi], inner, c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0],
+                                 c->active, outer_per_rep, c->g.pitch[gi]);
+  t_end(c, ax == 0 ? (sign < 0 ? K_FFT_Y_FWD : K_FFT_Y_INV) : (sign < 0 ? K_FFT_X_FWD : K_FFT_X_INV));
+  return e;
 }
 
 template <typename T>
-static cudaError_t launch_contract(pfdd_ctx *c) {
-  switch (c->ns) {
-    case 1: return launch_contract_ns<T, 1>(c);
-    case 2: return launch_contract_ns<T, 2>(c);
-    case 3: return launch_contract_ns<T, 3>(c);
-    case 4: return launch_contract_ns<T, 4>(c);
-    case 5: return launch_contract_ns<T, 5>(c);
-    case 6: return launch_contract_ns<T, 6>(c);
-    case 7: return launch_contract_ns<T, 7>(c);
-    case 8: return launch_contract_ns<T, 8>(c);
-    case 9: return launch_contract_ns<T, 9>(c);
-    case 10: return launch_contract_ns<T, 10>(c);
-    case 11: return launch_contract_ns<T, 11>(c);
-    case 12: return launch_contract_ns<T, 12>(c);
-    default: return cudaErrorInvalidValue;
-  }
+static cudaError_t launch_x_fused(pfdd_ctx *c) {
+  XParams xp;
+  xp.S = c->S; xp.B = c->B; xp.active = c->active; xp.tw = c->tw[0];
+  xp.inner = (long long)c->n[1] * c->n[2]; xp.tiles = c->g.xTiles;
+  xp.L = c->n[0]; xp.lgL = ilog2(c->n[0]); xp.lgT = c->g.xLgT; xp.pitch = c->g.xPitch; xp.R = c->nrep;
+  const unsigned blocks = (unsigned)(c->nrep * c->g.xTiles);
+  t_begin(c);
+  cudaError_t e = std::is_same<T, float>::value
+                      ? launch_x_fused_f32(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
+                      : launch_x_fused_f64(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp);
+  t_end(c, K_X_FUSED);
+  return e;
 }
 
 template <typename T>
@@ -514,7 +658,7 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
   zp.active = c->active;
   zp.tw = c->tw[2];
   zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
-  zp.L = c->n[2]; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
+  zp.L = c->n[2]; zp.lgL = c->g.lgL3; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
   zp.pitch = c->g.zPitch;
   zp.inv_n = 1.0 / (double)c->N;  // N is a power of two: exact, same as dividing by nsize
   zp.uq2 = c->uq2;
@@ -525,7 +669,7 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
   }
   const int RF = c->nrep * c->ns;
   if (!c->specValid) {
-    CK(c, launch_zpass<T>(c, zp, Z_SRC_XI | Z_FWD | Z_STORE));
+    CK(c, ctx_zpass(c, zp, Z_SRC_XI | Z_FWD | Z_STORE));
     c->specValid = true;
   }
   for (int s0 = 0; s0 < nsteps; s0 += c->kchunk) {
@@ -539,18 +683,16 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
         }
     CK(c, cudaMemcpyAsync(c->tau, c->h_tau, (size_t)ks * RF * sizeof(double), cudaMemcpyHostToDevice, c->st));
     for (int s = 0; s < ks; ++s) {
-      CK(c, (launch_strided<T, -1>(c, 0)));
-      CK(c, (launch_strided<T, -1>(c, 1)));
-      CK(c, launch_contract<T>(c));
-      CK(c, (launch_strided<T, +1>(c, 1)));
-      CK(c, (launch_strided<T, +1>(c, 0)));
+      CK(c, ctx_strided(c, -1, 0));
+      CK(c, launch_x_fused<T>(c));
+      CK(c, ctx_strided(c, +1, 0));
       zp.step = s;
-      CK(c, launch_zpass<T>(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE));
+      CK(c, ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE));
     }
     const int nt = ks * c->nrep;
     t_begin(c);
-    gamma_reduce_kernel<<<(nt + 127) / 128, 128, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, ks, zp.inv_n,
-                                                             c->gam_a, c->gam);
+    gamma_reduce_kernel<<<nt, kThreads, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, zp.inv_n, c->gam_a,
+                                                    c->gam);
     t_end(c, K_GAMMA);
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(c->h_gam_a, c->gam_a, (size_t)ks * RF * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -640,11 +782,9 @@ extern "C" pfdd_status pfdd_fft_plan_create(pfdd_fft_plan **out, int n1, int n2,
   p->n[0] = n1; p->n[1] = n2; p->n[2] = n3;
   p->prec = precision; p->dev = device; p->max_batch = max_batch;
   p->N = (long long)n1 * n2 * n3;
-  p->g = make_geometry(n1, n2, n3, vsize_of(precision));
+  p->g = make_geometry(n1, n2, n3, 0, vsize_of(precision), bsize_of(precision));
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->st, cudaStreamNonBlocking);
-  const size_t maxsmem = std::max({p->g.zSmem, p->g.smem[0], p->g.smem[1]});
-  if (e == cudaSuccess) e = precision == PFDD_FP64 ? set_smem_attrs<double>(maxsmem) : set_smem_attrs<float>(maxsmem);
   if (e == cudaSuccess) e = cudaMalloc(&p->buf, (size_t)max_batch * p->N * vsize_of(precision));
   if (e == cudaSuccess) e = make_twiddles(p->tw, p->n, precision, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
@@ -667,14 +807,14 @@ extern "C" void pfdd_fft_plan_destroy(pfdd_fft_plan *p) {
   delete p;
 }
 
-template <typename T>
 static cudaError_t fft_exec(pfdd_fft_plan *p, void *dbuf, int batch, int sign) {
   const Geometry &g = p->g;
+  const int pc = prec_code(p->prec);
   ZParams zp;
   std::memset(&zp, 0, sizeof zp);
   zp.S = dbuf; zp.tw = p->tw[2]; zp.N = p->N; zp.lines_per_field = (long long)p->n[0] * p->n[1];
-  zp.L = p->n[2]; zp.ns = batch; zp.R = 1; zp.TL = g.zTL; zp.nparts = g.zNparts; zp.pitch = g.zPitch;
-  const long long zblocks = (long long)batch * g.zNparts;
+  zp.L = p->n[2]; zp.lgL = g.lgL3; zp.ns = batch; zp.R = 1; zp.TL = g.zTL; zp.nparts = g.zNparts; zp.pitch = g.zPitch;
+  const unsigned zblocks = (unsigned)((long long)batch * g.zNparts);
   auto strided = [&](int ax, int s) -> cudaError_t {
     const int L = ax == 0 ? p->n[1] : p->n[0];
     if (L == 1) return cudaSuccess;
@@ -682,27 +822,20 @@ static cudaError_t fft_exec(pfdd_fft_plan *p, void *dbuf, int batch, int sign) {
     const long long inner = ax == 0 ? (long long)p->n[2] : (long long)p->n[1] * p->n[2];
     const long long outer = ax == 0 ? (long long)batch * p->n[0] : (long long)batch;
     const long long blocks = outer * g.tiles[gi];
-    if (s < 0)
-      fft_strided_kernel<T, -1><<<(unsigned)blocks, g.threads[gi], g.smem[gi], p->st>>>(
-          dbuf, L, inner, g.TI[gi], g.tiles[gi], p->tw[ax == 0 ? 1 : 0], nullptr, outer, g.pitch[gi]);
-    else
-      fft_strided_kernel<T, +1><<<(unsigned)blocks, g.threads[gi], g.smem[gi], p->st>>>(
-          dbuf, L, inner, g.TI[gi], g.tiles[gi], p->tw[ax == 0 ? 1 : 0], nullptr, outer, g.pitch[gi]);
-    return cudaGetLastError();
+    return launch_strided(pc, s, ilog2(L), (unsigned)blocks, g.threads[gi], g.smem[gi], p->st, dbuf, g.lgTI[gi], inner,
+                          g.tiles[gi], p->tw[ax == 0 ? 1 : 0], nullptr, outer, g.pitch[gi]);
   };
   cudaError_t e;
   if (sign < 0) {
     zp.flags = Z_FWD | Z_STORE;
-    zpass_kernel<T><<<(unsigned)zblocks, g.zThreads, g.zSmem, p->st>>>(zp);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_zpass(pc, g.lgL3, zblocks, g.zThreads, g.zSmem, p->st, zp)) != cudaSuccess) return e;
     if ((e = strided(0, -1)) != cudaSuccess) return e;
     return strided(1, -1);
   }
   if ((e = strided(1, +1)) != cudaSuccess) return e;
   if ((e = strided(0, +1)) != cudaSuccess) return e;
   zp.flags = Z_INV | Z_STORE;
-  zpass_kernel<T><<<(unsigned)zblocks, g.zThreads, g.zSmem, p->st>>>(zp);
-  return cudaGetLastError();
+  return launch_zpass(pc, g.lgL3, zblocks, g.zThreads, g.zSmem, p->st, zp);
 }
 
 static pfdd_status fft_call(pfdd_fft_plan *p, void *data, int batch, int on_device, int sign) {
@@ -712,7 +845,7 @@ static pfdd_status fft_call(pfdd_fft_plan *p, void *data, int batch, int on_devi
   void *d = on_device ? data : p->buf;
   cudaError_t e = cudaSuccess;
   if (!on_device) e = cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, p->st);
-  if (e == cudaSuccess) e = p->prec == PFDD_FP64 ? fft_exec<double>(p, d, batch, sign) : fft_exec<float>(p, d, batch, sign);
+  if (e == cudaSuccess) e = fft_exec(p, d, batch, sign);
   if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
   return e == cudaSuccess ? PFDD_OK : PFDD_ECUDA;

@@ -6,9 +6,10 @@
 // positions th + m*L/8 (m = 0..7), applies the stage twiddles, runs radix-8
 // (or two radix-4, or four radix-2) butterflies in registers and writes the
 // results back in Stockham (self-sorting) order, so the final stage leaves the
-// transform in natural order.  Signs follow the reference's fft_forward /
-// fft_backward (PFDD_Final_GPU.c:209-273): forward exp(-2 pi i nk/L),
-// backward exp(+2 pi i nk/L), no normalisation.
+// transform in natural order.  All index arithmetic is shifts and masks; the
+// twiddles come from a table in shared memory.  Signs follow the reference's
+// fft_forward / fft_backward (PFDD_Final_GPU.c:209-273): forward
+// exp(-2 pi i nk/L), backward exp(+2 pi i nk/L), no normalisation.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -74,14 +75,19 @@ template <int S, typename V> __device__ __forceinline__ void dft8(V *x) {
   x[3] = cadd(e3, o3); x[7] = csub(e3, o3);
 }
 
-// One Stockham stage of radix R (R in {2,4,8}) for a team thread th holding
-// v[m] = line[th + m*L/8].  Ns = product of the radices already applied.
-// sm(l) addresses element l of this thread's line in shared memory.
+// Padded position of element l in a contiguous line: one pad slot per 8
+// elements, so the stride-8 writes of the first radix-8 stage hit distinct banks.
+__device__ __forceinline__ int pad8(int l) { return l + (l >> 3); }
+
+// One Stockham stage of radix R = 2^lgR for a team thread th holding
+// v[m] = line[th + m*L/8].  Ns = 2^lgNs radices already applied.
 template <int S, int R, typename V, typename Addr>
-__device__ __forceinline__ void stockham_stage(V *v, int th, int L, int Ns, const V *__restrict__ tw, Addr sm) {
+__device__ __forceinline__ void stockham_stage(V *v, int th, int lgL, int lgNs, const V *tw, Addr sm) {
   constexpr int NB = 8 / R;  // butterflies per thread
-  const int L8 = L >> 3;
-  const int LR = L / R;
+  constexpr int lgR = R == 8 ? 3 : (R == 4 ? 2 : 1);
+  const int L8 = 1 << (lgL - 3);
+  const int Ns = 1 << lgNs;
+  const int tsh = lgL - lgNs - lgR;  // twiddle index step = k << tsh
 #pragma unroll
   for (int u = 0; u < NB; ++u) {
     const int j = th + u * L8;
@@ -89,30 +95,36 @@ __device__ __forceinline__ void stockham_stage(V *v, int th, int L, int Ns, cons
     V a[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) a[r] = v[u + r * NB];
-    if (Ns > 1) {
-      const int tstep = k * (L / (Ns * R));
+    if (lgNs > 0) {
+      const int ts = k << tsh;
 #pragma unroll
-      for (int r = 1; r < R; ++r) a[r] = ctw<S>(a[r], __ldg(&tw[r * tstep]));
+      for (int r = 1; r < R; ++r) a[r] = ctw<S>(a[r], tw[r * ts]);
     }
     if (R == 8) dft8<S>(a);
     else if (R == 4) dft4<S>(a[0], a[1], a[2], a[3]);
     else dft2<S>(a[0], a[1]);
-    const int base = (j - k) * R + k;  // (j / Ns) * Ns * R + k
+    const int base = ((j - k) << lgR) + k;  // (j / Ns) * Ns * R + k
 #pragma unroll
-    for (int q = 0; q < R; ++q) *sm(base + q * Ns) = a[q];
+    for (int q = 0; q < R; ++q) *sm(base + (q << lgNs)) = a[q];
   }
-  (void)LR;
 }
 
 // Full transform of the team's line, data in shared memory in natural order
-// before and after.  Every thread of the block must call it (it synchronises).
-template <int S, typename V, typename Addr>
-__device__ __forceinline__ void line_fft(int th, int L, const V *__restrict__ tw, Addr sm, bool active) {
-  if (L >= 8) {
-    const int L8 = L >> 3;
-    int Ns = 1;
-    while (Ns < L) {
-      const int rem = L / Ns;
+// before and after; sm(l) addresses element l.  tw: forward twiddles of
+// length L (shared memory).  Every thread of the block must call it.
+// LG >= 0 fixes log2(L) at compile time (stage loop unrolled, all index
+// arithmetic folded); LG < 0 takes it from lgL at run time.
+template <int S, int LG, typename V, typename Addr>
+__device__ __forceinline__ void line_fft(int th, int lgL_rt, const V *tw, Addr sm, bool active) {
+  const int lgL = LG >= 0 ? LG : lgL_rt;
+  if (lgL >= 3) {
+    const int L8 = 1 << (lgL - 3);
+    constexpr int NST = LG >= 0 ? (LG + 2) / 3 : 4;  // stage count (run time: at most 4 for L <= 4096)
+#pragma unroll
+    for (int st = 0; st < NST; ++st) {
+      const int lgNs = 3 * st;  // every stage before the last is radix 8
+      if (LG < 0 && lgNs >= lgL) break;
+      const int rem = lgL - lgNs;
       V v[8];
       if (active) {
 #pragma unroll
@@ -120,16 +132,15 @@ __device__ __forceinline__ void line_fft(int th, int L, const V *__restrict__ tw
       }
       __syncthreads();
       if (active) {
-        if (rem >= 8) stockham_stage<S, 8>(v, th, L, Ns, tw, sm);
-        else if (rem == 4) stockham_stage<S, 4>(v, th, L, Ns, tw, sm);
-        else stockham_stage<S, 2>(v, th, L, Ns, tw, sm);
+        if (rem >= 3) stockham_stage<S, 8>(v, th, lgL, lgNs, tw, sm);
+        else if (rem == 2) stockham_stage<S, 4>(v, th, lgL, lgNs, tw, sm);
+        else stockham_stage<S, 2>(v, th, lgL, lgNs, tw, sm);
       }
       __syncthreads();
-      Ns *= (rem >= 8 ? 8 : rem);
     }
-  } else if (L == 4 || L == 2) {
+  } else if (lgL >= 1) {
     if (active) {
-      if (L == 4) {
+      if (lgL == 2) {
         V a0 = *sm(0), a1 = *sm(1), a2 = *sm(2), a3 = *sm(3);
         dft4<S>(a0, a1, a2, a3);
         *sm(0) = a0; *sm(1) = a1; *sm(2) = a2; *sm(3) = a3;
@@ -141,6 +152,30 @@ __device__ __forceinline__ void line_fft(int th, int L, const V *__restrict__ tw
     }
     __syncthreads();
   }
+}
+
+// Copies a length-L twiddle table to shared memory (caller synchronises).
+template <typename V>
+__device__ __forceinline__ void load_twiddles(V *dst, const V *__restrict__ src, int L) {
+  for (int i = threadIdx.x; i < L; i += blockDim.x) dst[i] = src[i];
+}
+
+// ---- asynchronous global -> shared copies (cp.async, completion groups) ----
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <typename V> __device__ __forceinline__ void cp_async_elem(V *smem, const V *gmem) {
+  if (sizeof(V) == 16) cp_async16(smem, gmem);
+  else cp_async8(smem, gmem);
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 }  // namespace pfdd

@@ -1,19 +1,21 @@
-// pfdd_kernels.cuh -- kernels of the PFDD TDGL step (generic path, any
-// power-of-two grid, FP64 or FP32 spectral precision).
+// pfdd_kernels.cuh -- kernels of the PFDD TDGL step (any power-of-two grid,
+// FP64 or FP32 spectral precision).
 //
 // Device data (N = N1*N2*N3, R replicas, ns slip systems):
 //   xi   double2 [R][ns][N]   order parameter, FP64 state (F:4146)
 //   S    T2      [R][ns][N]   spectral work buffer (T = double or float)
-//   B    T       [P][N]       packed symmetric B(k), P = ns(ns+1)/2 pairs
-//                             a <= b in row-major order
+//   B    T       packed symmetric B(k), P = ns(ns+1)/2 pairs a <= b in
+//                row-major order, stored in the tile order of the fused
+//                x-pass (see BLayout) so each tile streams one contiguous block
 //   bc   uint32  bit mask     bit (r*ns+a)*N+pt set = pinned (xi_bc != 0)
 //
-// One TDGL step of the generic path is six launches:
-//   y-forward, x-forward, contraction, x-inverse, y-inverse,
-//   z-pass (z-inverse -> Euler update + gamma partials -> z-forward).
-// The z-forward of the new state is fused into the update so S always holds
-// the z-transformed state between steps.
+// One TDGL step is four launches:
+//   y-forward FFT, x-pass (x-forward FFT -> B(k) contraction -> x-inverse FFT),
+//   y-inverse FFT, z-pass (z-inverse FFT -> Euler update + gamma partials ->
+//   z-forward FFT of the new state).
+// S therefore holds the z-transformed state between steps.
 #pragma once
+#include "pfdd_convert.cuh"
 #include "pfdd_fft.cuh"
 
 namespace pfdd {
@@ -38,37 +40,43 @@ struct ZParams {
   const uint8_t *active;    // [R] or null
   const void *tw;           // forward twiddles of length L
   long long N, lines_per_field;
-  int step, L, ns, R, TL, nparts, flags, pitch;
+  int step, L, lgL, ns, R, TL, nparts, flags, pitch;
   double inv_n, uq2;
   double cd2[kMaxNs], asf_pi[kMaxNs], uq2cd2[kMaxNs];
 };
 
 template <typename V> __device__ __forceinline__ V from_xi(double2 x);
 template <> __device__ __forceinline__ double2 from_xi<double2>(double2 x) { return x; }
-template <> __device__ __forceinline__ float2 from_xi<float2>(double2 x) { return make_float2((float)x.x, (float)x.y); }
+template <> __device__ __forceinline__ float2 from_xi<float2>(double2 x) {
+  return make_float2(f64_to_f32_int(x.x), f64_to_f32_int(x.y));
+}
 
-// plasticevolv (F:3470-3501) for one point.  FP64 form: the reference's
-// expression in double precision.  FP32 form: force and core term evaluated
-// in FP32 (sin of an FP64-reduced argument), then accumulated into the FP64
-// state.
+// plasticevolv (F:3470-3501) for one point, plain FP64 form: the reference's
+// expression in double precision (pi truncated as F:95).
 __device__ __forceinline__ void tdgl_point(double2 &x, double2 f, double cd2, double asf_pi, double uq2,
                                            double uq2cd2, double ctau, double inv_n) {
   const double s = sinpi(x.x * kTwoPiTruncOverPi);
   x.x = x.x - cd2 * (uq2 * f.x * inv_n + asf_pi * s - ctau);
   x.y = x.y - uq2cd2 * (f.y * inv_n);
 }
-__device__ __forceinline__ void tdgl_point(double2 &x, float2 f, double cd2, double asf_pi, double uq2,
-                                           double uq2cd2, double ctau, double inv_n) {
-  const double nr = rint(x.x);
-  const float r = (float)(x.x - nr);
-  const float s = sinpif(2.0f * r);
-  const float fi = (float)inv_n;
-  const float inner = (float)uq2 * f.x * fi + (float)asf_pi * s - (float)ctau;
-  const float dre = (float)cd2 * inner;
-  const float dim = (float)uq2cd2 * (f.y * fi);
-  x.x = x.x - (double)dre;
-  x.y = x.y - (double)dim;
-}
+// FP32-FFT form (inlined in the z-pass): the increment -- force, core term
+// on the FP32-rounded state, stress -- is evaluated in FP32, then subtracted
+// from the FP64 state; the FP64 <-> FP32 conversions run on the integer pipe.
+
+template <typename T> struct UpdCoef;
+template <> struct UpdCoef<double> {
+  double cd2, asf_pi, uq2, uq2cd2, inv_n;
+  __device__ UpdCoef(const ZParams &p, int a) : cd2(p.cd2[a]), asf_pi(p.asf_pi[a]), uq2(p.uq2), uq2cd2(p.uq2cd2[a]),
+                                                inv_n(p.inv_n) {}
+  __device__ double tau(double t) const { return t; }
+};
+template <> struct UpdCoef<float> {
+  float cd2, asf_pi, uq2, uq2cd2, inv_n;
+  __device__ UpdCoef(const ZParams &p, int a)
+      : cd2((float)p.cd2[a]), asf_pi((float)p.asf_pi[a]), uq2((float)p.uq2), uq2cd2((float)p.uq2cd2[a]),
+        inv_n((float)p.inv_n) {}
+  __device__ float tau(double t) const { return (float)t; }
+};
 
 __device__ __forceinline__ double block_sum(double v, double *red) {
 #pragma unroll
@@ -85,166 +93,322 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
   return s;
 }
 
+// Exact accumulation of FP64 values in 64-bit fixed point with 2^-44
+// resolution, on the integer pipe (FP64 adds run at 1/58 of the FP32 rate on
+// GB300).  round(d * 2^44) is formed from the bit pattern; |d| must stay below
+// 2^7 so that the 2048 values of one block cannot overflow (anything larger,
+// or non-finite, raises `big`, which the caller turns into a NaN partial: the
+// divergence watchdog).  The sums are exact, hence independent of the order.
+constexpr int kFixBits = 44;
+__device__ __forceinline__ long long to_fixed_bits(unsigned long long u, bool &big) {
+  const int e = (int)((u >> 52) & 0x7ff);
+  if (e >= 1023 + 7) { big = true; return 0; }
+  const int sh = 1075 - kFixBits - e;  // |d| = m * 2^(e-1075) = (m >> sh) units of 2^-44
+  if (e == 0 || sh >= 64) return 0;
+  const unsigned long long m = (u & 0xfffffffffffffull) | (1ull << 52);
+  const long long v = sh > 0 ? (long long)((m + (1ull << (sh - 1))) >> sh) : (long long)(m << (-sh));
+  return (u >> 63) ? -v : v;
+}
+__device__ __forceinline__ long long to_fixed(double d, bool &big) {
+  return to_fixed_bits((unsigned long long)__double_as_longlong(d), big);
+}
+
+__device__ __forceinline__ long long block_sum_i64(long long v, long long *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  long long s = 0;
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int i = 0; i < nw; ++i) s += red[i];
+  }
+  return s;
+}
+
 // z-pass: TL contiguous lines of length L (one field), see ZFlags.
-template <typename T>
+// Shared memory: twiddles [L] | S lines [TL][pitch] (padded) | xi tile
+// [TL*L] double2 (update only).  The S lines and the xi tile are fetched with
+// cp.async in two completion groups so the xi fetch overlaps the inverse FFT.
+template <typename T, int LG>
 __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ double red[32];
-  V *sm = reinterpret_cast<V *>(smraw);
-  const int L = p.L, TL = p.TL, P = p.pitch;
+  __shared__ long long red[32];
+  const int L = p.L, lgL = p.lgL, TL = p.TL, P = p.pitch;
+  V *tws = reinterpret_cast<V *>(smraw);
+  V *sm = tws + L;
+  double2 *xs = reinterpret_cast<double2 *>(smraw + ((((size_t)L + (size_t)TL * P) * sizeof(V) + 15) & ~(size_t)15));
   const int E = L >= 8 ? 8 : L, team = L / E;
   const long long line0 = (long long)blockIdx.x * TL;
   const long long rf = line0 / p.lines_per_field;
   const int r = (int)(rf / p.ns), a = (int)(rf % p.ns);
   if (p.active && !p.active[r]) return;
   const long long lf0 = line0 - rf * p.lines_per_field;
-  const long long e0 = line0 * L;
-  const int nel = TL * L;
+  const long long e0 = line0 << lgL;
+  const int nel = TL << lgL;
   const int tid = threadIdx.x, nthr = blockDim.x;
   V *S = reinterpret_cast<V *>(p.S);
-  const V *tw = reinterpret_cast<const V *>(p.tw);
+  const bool upd = (p.flags & Z_UPDATE) != 0;
+  auto sidx = [&](int e) { return (e >> lgL) * P + pad8(e & (L - 1)); };
 
+  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   if (p.flags & Z_SRC_XI) {
-    for (int e = tid; e < nel; e += nthr) sm[(e / L) * P + (e % L)] = from_xi<V>(p.xi[e0 + e]);
+    for (int e = tid; e < nel; e += nthr) sm[sidx(e)] = from_xi<V>(p.xi[e0 + e]);
   } else {
-    for (int e = tid; e < nel; e += nthr) sm[(e / L) * P + (e % L)] = S[e0 + e];
+    for (int e = tid; e < nel; e += nthr) cp_async_elem(&sm[sidx(e)], &S[e0 + e]);
   }
+  cp_async_commit();
+  if (upd) {
+    for (int e = tid; e < nel; e += nthr) cp_async16(&xs[e], &p.xi[e0 + e]);
+  }
+  cp_async_commit();
+  cp_async_wait<1>();
   __syncthreads();
   const int t = tid / team, th = tid - t * team;
   const bool act = t < TL;
-  auto line = [&](int l) { return &sm[t * P + l]; };
-  if (p.flags & Z_INV) line_fft<+1>(th, L, tw, line, act);
+  auto line = [&](int l) { return &sm[t * P + pad8(l)]; };
+  if (p.flags & Z_INV) line_fft<+1, LG>(th, lgL, tws, line, act);
 
-  if (p.flags & Z_UPDATE) {
-    const double cd2 = p.cd2[a], asf_pi = p.asf_pi[a], uq2cd2 = p.uq2cd2[a];
+  if (upd) {
+    cp_async_wait<0>();
+    __syncthreads();
+    const UpdCoef<T> k(p, a);
     const double tv = p.tau[((long long)p.step * p.R + r) * p.ns + a];
+    const auto ctau0 = k.tau(tv);
     const long long fbase = rf * p.N;  // bit / element base of this field
-    double acc = 0.0;
-    for (int e = tid; e < nel; e += nthr) {
-      V *sp = &sm[(e / L) * P + (e % L)];
-      double2 x = p.xi[e0 + e];
-      const long long pt = lf0 * L + e;
-      bool evolve = true;
-      if (p.bc) {
-        const long long bit = fbase + pt;
-        evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
+    long long acc = 0;
+    bool big = false;
+    if constexpr (sizeof(V) == sizeof(float2)) {
+      // FP32-FFT form: the FP64 state stays in integer registers as bit
+      // patterns; FP64 arithmetic is exactly the two subtractions (the
+      // compiler otherwise routes 64-bit register moves through the FP64 pipe).
+      const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xs);
+      ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(p.xi) + e0;
+      for (int e = tid; e < nel; e += nthr) {
+        V *sp = &sm[sidx(e)];
+        ulonglong2 xb = xsb[e];
+        const long long pt = (lf0 << lgL) + e;
+        bool evolve = true;
+        if (p.bc) {
+          const long long bit = fbase + pt;
+          evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
+        }
+        if (evolve) {
+          float ctau = ctau0;
+          if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
+          const float2 f = *sp;
+          const float xr = f64bits_to_f32_int(xb.x);
+          const float s = sinpif(2.0f * xr);
+          const float dre = k.cd2 * (k.uq2 * f.x * k.inv_n + k.asf_pi * s - ctau);
+          const float dim = k.uq2cd2 * (f.y * k.inv_n);
+          xb.x = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.x) -
+                                                          __longlong_as_double((long long)f32_to_f64bits_int(dre)));
+          xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
+                                                          __longlong_as_double((long long)f32_to_f64bits_int(dim)));
+          xg[e] = xb;
+        }
+        acc += to_fixed_bits(xb.x, big);
+        V o;
+        o.x = f64bits_to_f32_int(xb.x);
+        o.y = f64bits_to_f32_int(xb.y);
+        *sp = o;
       }
-      if (evolve) {
-        double ctau = tv;
-        if (p.tau_field) ctau = (p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a];
-        tdgl_point(x, *sp, cd2, asf_pi, p.uq2, uq2cd2, ctau, p.inv_n);
-        p.xi[e0 + e] = x;
+    } else {
+      for (int e = tid; e < nel; e += nthr) {
+        V *sp = &sm[sidx(e)];
+        double2 x = xs[e];
+        const long long pt = (lf0 << lgL) + e;
+        bool evolve = true;
+        if (p.bc) {
+          const long long bit = fbase + pt;
+          evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
+        }
+        if (evolve) {
+          auto ctau = ctau0;
+          if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
+          tdgl_point(x, *sp, k.cd2, k.asf_pi, k.uq2, k.uq2cd2, ctau, k.inv_n);
+          p.xi[e0 + e] = x;
+        }
+        acc += to_fixed(x.x, big);
+        *sp = from_xi<V>(x);
       }
-      acc += x.x;
-      *sp = from_xi<V>(x);
     }
-    const double s = block_sum(acc, red);
-    if (tid == 0) p.part[((long long)p.step * p.R * p.ns + rf) * p.nparts + lf0 / TL] = s;
+    const long long s = block_sum_i64(acc, red);
+    const int anybig = __syncthreads_or(big);
+    if (tid == 0)
+      p.part[((long long)p.step * p.R * p.ns + rf) * p.nparts + lf0 / TL] =
+          anybig ? __longlong_as_double(0x7ff8000000000000ll) : (double)s * 0x1p-44;
     __syncthreads();
   }
 
-  if (p.flags & Z_FWD) line_fft<-1>(th, L, tw, line, act);
+  if (p.flags & Z_FWD) line_fft<-1, LG>(th, lgL, tws, line, act);
   if (p.flags & Z_STORE) {
     if (L < 8) __syncthreads();
-    for (int e = tid; e < nel; e += nthr) S[e0 + e] = sm[(e / L) * P + (e % L)];
+    for (int e = tid; e < nel; e += nthr) S[e0 + e] = sm[sidx(e)];
   }
 }
 
 // Batched line FFT along a strided axis: data viewed as [outer][L][inner],
 // one CTA transforms an L x TI tile (TI contiguous inner columns).
-template <typename T, int S>
+// Shared memory: twiddles [L] | tile [L][pitch].
+template <typename T, int S, int LG>
 __global__ void __launch_bounds__(256)
-fft_strided_kernel(void *data_, int L, long long inner, int TI, long long tiles_per_outer, const void *tw_,
+fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long tiles_per_outer, const void *tw_,
                    const uint8_t *active, long long outer_per_rep, int pitch) {
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
-  V *sm = reinterpret_cast<V *>(smraw);
+  const int L = 1 << lgL, TI = 1 << lgTI;
+  V *tws = reinterpret_cast<V *>(smraw);
+  V *sm = tws + L;
   const long long o = blockIdx.x / tiles_per_outer;
-  const long long c0 = (blockIdx.x - o * tiles_per_outer) * (long long)TI;
+  const long long c0 = (blockIdx.x - o * tiles_per_outer) << lgTI;
   if (active && !active[o / outer_per_rep]) return;
   V *base = reinterpret_cast<V *>(data_) + o * (long long)L * inner + c0;
-  const V *tw = reinterpret_cast<const V *>(tw_);
-  const int nel = L * TI, tid = threadIdx.x, nthr = blockDim.x;
+  const int nel = L << lgTI, tid = threadIdx.x, nthr = blockDim.x;
+  load_twiddles(tws, reinterpret_cast<const V *>(tw_), L);
   for (int e = tid; e < nel; e += nthr) {
-    const int l = e / TI, t = e - l * TI;
-    sm[l * pitch + t] = base[(long long)l * inner + t];
+    const int l = e >> lgTI, t = e & (TI - 1);
+    cp_async_elem(&sm[l * pitch + t], &base[(long long)l * inner + t]);
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   const int E = L >= 8 ? 8 : L, team = L / E;
-  const int t = tid % TI, th = tid / TI;
+  const int t = tid & (TI - 1), th = tid >> lgTI;
   const bool act = th < team;
-  line_fft<S>(th, L, tw, [&](int l) { return &sm[l * pitch + t]; }, act);
+  line_fft<S, LG>(th, lgL, tws, [&](int l) { return &sm[l * pitch + t]; }, act);
   for (int e = tid; e < nel; e += nthr) {
-    const int l = e / TI, tt = e - l * TI;
+    const int l = e >> lgTI, tt = e & (TI - 1);
     base[(long long)l * inner + tt] = sm[l * pitch + tt];
   }
 }
 
-// k-space contraction (F:4609-4629): S[r][a](k) <- sum_b B_ab(k) S[r][b](k),
-// b ascending for every a, RC replicas per pass so each B value is loaded once
-// per RC replicas.
-template <typename T, int NS, int RC>
-__global__ void __launch_bounds__(256)
-contract_kernel(void *S_, const T *__restrict__ B, long long N, int R, const uint8_t *active) {
-  using V = typename cpx<T>::t;
-  V *S = reinterpret_cast<V *>(S_);
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
-    for (int r0 = 0; r0 < R; r0 += RC) {
-      V in[RC][NS], out[RC][NS];
-      bool on[RC];
-#pragma unroll
-      for (int q = 0; q < RC; ++q) {
-        on[q] = (r0 + q < R) && (!active || active[r0 + q]);
-#pragma unroll
-        for (int b = 0; b < NS; ++b) {
-          in[q][b] = on[q] ? S[((long long)(r0 + q) * NS + b) * N + pt] : V{0, 0};
-          out[q][b] = V{0, 0};
-        }
-      }
-      int pidx = 0;
-#pragma unroll
-      for (int a = 0; a < NS; ++a) {
-#pragma unroll
-        for (int b = a; b < NS; ++b, ++pidx) {
-          const T v = __ldg(&B[(long long)pidx * N + pt]);
-#pragma unroll
-          for (int q = 0; q < RC; ++q) {
-            out[q][a].x += in[q][b].x * v;
-            out[q][a].y += in[q][b].y * v;
-            if (b != a) {
-              out[q][b].x += in[q][a].x * v;
-              out[q][b].y += in[q][a].y * v;
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < RC; ++q)
-        if (on[q]) {
-#pragma unroll
-          for (int b = 0; b < NS; ++b) S[((long long)(r0 + q) * NS + b) * N + pt] = out[q][b];
-        }
-    }
-  }
+// Device order of B(k).  The fused x-pass tile c (T consecutive inner indices
+// j*N3+k, every x) holds B for its T*N1 points contiguously per pair:
+//   index = (c*P + p) * (T*N1) + t*N1 + x,  inner index = c*T + t.
+struct BLayout {
+  long long N, inner;
+  int L, lgT, P;
+};
+__host__ __device__ __forceinline__ long long b_index(const BLayout &bl, int p, long long pt) {
+  const long long x = pt / bl.inner, c = pt - x * bl.inner;
+  const long long tile = c >> bl.lgT, t = c & ((1LL << bl.lgT) - 1);
+  return (tile * bl.P + p) * ((long long)bl.L << bl.lgT) + t * bl.L + x;
 }
 
-// Deterministic second stage of the gamma sums: one thread per (step, replica).
-__global__ void gamma_reduce_kernel(const double *part, int nparts, int R, int ns, int nsteps, double inv_n,
-                                    double *gamma_a, double *gamma) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nsteps * R) return;
-  const int s = idx / R, r = idx - s * R;
-  double tot = 0.0;
-  for (int a = 0; a < ns; ++a) {
-    const double *pp = part + ((long long)s * R * ns + (long long)r * ns + a) * nparts;
-    double acc = 0.0;
-    for (int c = 0; c < nparts; ++c) acc += pp[c];
-    gamma_a[((long long)s * R + r) * ns + a] = acc * inv_n;
-    tot += acc;
+struct XParams {
+  void *S;
+  const void *B;
+  const uint8_t *active;
+  const void *tw;          // x-axis forward twiddles (length L = N1)
+  long long inner, tiles;  // inner = N2*N3, tiles = inner / T per field row
+  int L, lgL, lgT, pitch, R;
+};
+
+// Shared-memory bytes of the fused x-pass for a tile of T = 2^lgT.
+__host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, int pitch, size_t vsize,
+                                                        size_t bsize) {
+  const size_t head = ((size_t)L + (size_t)ns * ((size_t)1 << lgT) * pitch) * vsize;
+  const size_t P = (size_t)ns * (ns + 1) / 2;
+  return ((head + 15) & ~(size_t)15) + P * ((size_t)L << lgT) * bsize;
+}
+
+// Fused x-pass on a tile of T consecutive inner indices, all N1 x-values and
+// all NS fields of one replica: forward FFT along x, k-space contraction
+// S[a](k) <- sum_b B_ab(k) S[b](k) (F:4609-4629, b ascending), inverse FFT
+// along x.  Shared memory: twiddles [L] | tile [a][t][x] (x contiguous,
+// padded) | B tile [P][T*L].  The S tile and the B tile arrive by cp.async in
+// two groups, so the B fetch overlaps the forward FFT.  One point per thread
+// in the contraction; IN_REGS keeps its NS inputs in registers (FP32, up to
+// 384 threads); FP64 reads them from shared memory and runs at most 256 threads.
+template <typename T, int NS, bool IN_REGS, int LG>
+__global__ void __launch_bounds__(IN_REGS ? 384 : 256, 2) x_fused_kernel(XParams p) {
+  using V = typename cpx<T>::t;
+  constexpr int P = NS * (NS + 1) / 2;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int L = p.L, lgL = p.lgL, lgT = p.lgT, TT = 1 << lgT, LP = p.pitch;
+  V *tws = reinterpret_cast<V *>(smraw);
+  V *sm = tws + L;
+  const size_t head = (((size_t)L + (size_t)NS * TT * LP) * sizeof(V) + 15) & ~(size_t)15;
+  T *Bs = reinterpret_cast<T *>(smraw + head);
+  const long long r = blockIdx.x / p.tiles;
+  const long long tile = blockIdx.x - r * p.tiles;
+  if (p.active && !p.active[r]) return;
+  const long long c0 = tile << lgT;
+  const int npt = L << lgT;
+  V *S = reinterpret_cast<V *>(p.S);
+  const T *Bt = reinterpret_cast<const T *>(p.B) + tile * P * (long long)npt;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int nel = (NS * L) << lgT;
+  auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + pad8(x); };
+  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  // S tile: e -> (a, x, t) with t fastest (contiguous in memory)
+  for (int e = tid; e < nel; e += nthr) {
+    const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
+    cp_async_elem(&sm[sidx(a, t, x)], &S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t]);
   }
-  gamma[idx] = tot * inv_n;
+  cp_async_commit();
+  // B tile: one contiguous block of P * npt values
+  const int bbytes = P * npt * (int)sizeof(T);
+  if ((bbytes & 15) == 0) {
+    for (int i = tid; i < (bbytes >> 4); i += nthr)
+      cp_async16(reinterpret_cast<char *>(Bs) + 16 * i, reinterpret_cast<const char *>(Bt) + 16 * i);
+  } else {
+    for (int i = tid; i < P * npt; i += nthr) Bs[i] = Bt[i];
+  }
+  cp_async_commit();
+  cp_async_wait<1>();
+  __syncthreads();
+  const int E = L >= 8 ? 8 : L, team = L / E, teams = nthr / team;
+  const int lines = NS << lgT;
+  const int my_team = tid / team, th = tid - my_team * team;
+  for (int l0 = 0; l0 < lines; l0 += teams) {
+    const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+    line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int q = tid; q < npt; q += nthr) {
+    const int t = q >> lgL, x = q & (L - 1);
+    V out[NS];
+    V in[IN_REGS ? NS : 1];
+#pragma unroll
+    for (int a = 0; a < NS; ++a) {
+      out[a] = V{0, 0};
+      if (IN_REGS) in[a] = sm[sidx(a, t, x)];
+    }
+    int pidx = 0;
+#pragma unroll
+    for (int a = 0; a < NS; ++a) {
+      const V ina = IN_REGS ? in[a] : sm[sidx(a, t, x)];
+#pragma unroll
+      for (int b = a; b < NS; ++b, ++pidx) {
+        const T v = Bs[pidx * npt + q];
+        const V inb = IN_REGS ? in[b] : sm[sidx(b, t, x)];
+        out[a].x += inb.x * v;
+        out[a].y += inb.y * v;
+        if (b != a) {
+          out[b].x += ina.x * v;
+          out[b].y += ina.y * v;
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < NS; ++a) sm[sidx(a, t, x)] = out[a];
+  }
+  __syncthreads();
+  for (int l0 = 0; l0 < lines; l0 += teams) {
+    const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+    line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+  }
+  if (L < 8) __syncthreads();
+  for (int e = tid; e < nel; e += nthr) {
+    const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
+    S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t] = sm[sidx(a, t, x)];
+  }
 }
 
 // Forward twiddle table w[t] = exp(-2 pi i t / L), t < L (sincospi in FP64).
@@ -274,113 +438,6 @@ __device__ __forceinline__ double frec_dev(int i, int n, double d) {
   if (i >= 1 && i < n / 2) v = (double)(i) / (double)(n) / d;
   if (i >= n / 2) v = ((double)(i) - (double)(n)) / (double)(n) / d;
   return v;
-}
-
-// B(k) of Bmatrix (F:328-412) in closed form:
-//   B_ab = (E_ab - t_a^T G t_b) / mu,  t_a = sigma_a f,
-//   G_ki = (1/f^2) [delta_ik / (mu + mu' z_k)
-//                   - f_i f_k / f^2 / (mu + mu' z_i) / (mu + mu' z_k) (mu + lambda) / kk]
-// with z_i = f_i^2 / f^2 and kk = 1 + (mu + lambda) sum_j z_j / (mu + mu' z_j).
-__global__ void build_B_kernel(const BBuildParams *__restrict__ bp, double *Bd, float *Bf, long long N) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const int ns = bp->ns;
-  const long long P = (long long)ns * (ns + 1) / 2;
-  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
-    const int k3 = (int)(pt % bp->n3), k2 = (int)((pt / bp->n3) % bp->n2), k1 = (int)(pt / ((long long)bp->n3 * bp->n2));
-    const double f[3] = {frec_dev(k1, bp->n1, bp->d1), frec_dev(k2, bp->n2, bp->d2), frec_dev(k3, bp->n3, bp->d3)};
-    const double f2 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
-    if (!(f2 > 0)) {
-      for (long long q = 0; q < P; ++q) {
-        if (Bd) Bd[q * N + pt] = 0.0;
-        if (Bf) Bf[q * N + pt] = 0.0f;
-      }
-      continue;
-    }
-    const double mu = bp->mu, ll = bp->ll, mup = bp->mup;
-    double z[3], den[3];
-    for (int i = 0; i < 3; ++i) { z[i] = f[i] * f[i] / f2; den[i] = mu + mup * z[i]; }
-    const double kk = 1.0 + (mu + ll) * (1 / den[0] * z[0] + 1 / den[1] * z[1] + 1 / den[2] * z[2]);
-    double G[3][3];
-    for (int i = 0; i < 3; ++i)
-      for (int k = 0; k < 3; ++k)
-        G[i][k] = 1 / f2 * ((i == k ? 1.0 : 0.0) / den[k] - f[i] * f[k] / f2 / den[i] / den[k] * (mu + ll) / kk);
-    double t[kMaxNs][3], u[kMaxNs][3];
-    for (int a = 0; a < ns; ++a) {
-      for (int i = 0; i < 3; ++i)
-        t[a][i] = bp->sig[a][i][0] * f[0] + bp->sig[a][i][1] * f[1] + bp->sig[a][i][2] * f[2];
-      for (int i = 0; i < 3; ++i) u[a][i] = G[i][0] * t[a][0] + G[i][1] * t[a][1] + G[i][2] * t[a][2];
-    }
-    long long q = 0;
-    for (int a = 0; a < ns; ++a)
-      for (int b = a; b < ns; ++b, ++q) {
-        const double v = (bp->E[a][b] - (t[a][0] * u[b][0] + t[a][1] * u[b][1] + t[a][2] * u[b][2])) * bp->mu_inv;
-        if (Bd) Bd[q * N + pt] = v;
-        if (Bf) Bf[q * N + pt] = (float)v;
-      }
-  }
-}
-
-// Packs a host-layout B ([kb][ka][N], FP64) already on the device into the
-// pair layout, optionally rounding to FP32.
-__global__ void pack_B_kernel(const double *src, int ns, long long N, double *Bd, float *Bf) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
-    long long q = 0;
-    for (int a = 0; a < ns; ++a)
-      for (int b = a; b < ns; ++b, ++q) {
-        const double v = src[((long long)b * ns + a) * N + pt];
-        if (Bd) Bd[q * N + pt] = v;
-        if (Bf) Bf[q * N + pt] = (float)v;
-      }
-  }
-}
-
-// xi_bc -> pinned bit mask (bit set where xi_bc[..][0] != 0; the reference
-// evolves a point where XI_BC(...,0) == 0, F:3481).  `src` holds count
-// interleaved [re, im] pairs for bits bit0 .. bit0+count-1; each warp builds its
-// 32 bits with a ballot and merges them into at most two mask words.
-__global__ void pack_bc_kernel(const double *src, long long count, long long bit0, uint32_t *mask) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31LL; base < count; base += stride) {
-    const long long e = base + (threadIdx.x & 31);
-    const bool pin = e < count && src[2 * e] != 0.0;
-    const uint32_t bal = __ballot_sync(0xffffffffu, pin);
-    if ((threadIdx.x & 31) == 0) {
-      const long long n = count - base < 32 ? count - base : 32;
-      const long long b = bit0 + base;
-      const int sh = (int)(b & 31);
-      const unsigned long long m64 = (n == 32 ? 0xffffffffull : ((1ull << n) - 1)) << sh;
-      const unsigned long long p64 = ((unsigned long long)bal & (n == 32 ? 0xffffffffull : ((1ull << n) - 1))) << sh;
-      uint32_t *w = mask + (b >> 5);
-      atomicAnd(w, ~(uint32_t)m64);
-      atomicOr(w, (uint32_t)p64);
-      if (m64 >> 32) {
-        atomicAnd(w + 1, ~(uint32_t)(m64 >> 32));
-        atomicOr(w + 1, (uint32_t)(p64 >> 32));
-      }
-    }
-  }
-}
-
-__global__ void mask_any_kernel(const uint32_t *mask, long long words, int *any) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  int found = 0;
-  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += stride) found |= mask[w] != 0u;
-  if (__syncthreads_or(found) && threadIdx.x == 0) atomicOr(any, 1);
-}
-
-// Inverse of pack_B_kernel: pair layout (FP64 or FP32) -> [kb][ka][N] FP64.
-__global__ void unpack_B_kernel(const double *Bd, const float *Bf, int ns, long long N, double *dst) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += stride) {
-    long long q = 0;
-    for (int a = 0; a < ns; ++a)
-      for (int b = a; b < ns; ++b, ++q) {
-        const double v = Bd ? Bd[q * N + pt] : (double)Bf[q * N + pt];
-        dst[((long long)b * ns + a) * N + pt] = v;
-        dst[((long long)a * ns + b) * N + pt] = v;
-      }
-  }
 }
 
 }  // namespace pfdd

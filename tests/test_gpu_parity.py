@@ -39,7 +39,7 @@ def rel(a, b):
 def test_fp64_matches_reference_golden(native_lib, name):
     spec, z = load_golden(name)
     xf, g, ga, launches = run_gpu(spec)
-    assert launches >= spec.steps * 6
+    assert launches >= spec.steps * 4
     assert rel(g, z["gamma"]) <= GAMMA_RTOL
     assert np.max(np.abs(ga - z["gamma_a"])) <= GAMMA_RTOL * max(1e-3, np.max(np.abs(z["gamma_a"])))
     flat = xf.reshape(spec.ns, -1)
