@@ -44,7 +44,8 @@ typedef enum {
   PFDD_ECUDA = 3,       /* a CUDA runtime call failed; see pfdd_last_error */
   PFDD_ETIMEOUT = 4,    /* a bounded device-side wait ran out */
   PFDD_ENONFINITE = 5,  /* the state became NaN/Inf (divergence watchdog) */
-  PFDD_ENOTREADY = 6    /* a required input (B, parameters, state) was not set */
+  PFDD_ENOTREADY = 6,   /* a required input (B, parameters, state) was not set */
+  PFDD_ELIMIT = 7       /* size beyond a fixed capacity (pfdd_fft_device_noalloc) */
 } pfdd_status;
 
 typedef enum {
@@ -156,6 +157,25 @@ void pfdd_fft_plan_destroy(pfdd_fft_plan *plan);
  * double for FP64 plans. */
 pfdd_status pfdd_fft_forward(pfdd_fft_plan *plan, void *data, int batch, int on_device);
 pfdd_status pfdd_fft_backward(pfdd_fft_plan *plan, void *data, int batch, int on_device);
+
+/* In-place 3D C2C transform (fft_forward sign = -1, fft_backward sign = +1,
+ * unnormalised) of `batch` fields of 2*N values on the device, enqueued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) -- without any device
+ * allocation.  No counterpart in the reference: it exists for callers that
+ * cannot allocate device memory themselves, such as code inside an OpenACC
+ * data region whose device memory belongs to the OpenACC runtime, or a
+ * process held to a fixed device-memory budget.  Its only scratch, the twiddle
+ * tables, is one static device array in the library (24 KB, held by every GPU
+ * that loads the library until the process exits), so N1, N2, N3 are limited
+ * to powers of two <= 512: larger sizes return PFDD_ELIMIT, other invalid
+ * arguments PFDD_EINVAL.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array and each rewrites it before use, so calls that overlap on
+ * the GPU (different streams, or different threads) race: serialise them.
+ * The call returns after enqueueing; synchronise `stream` before reading
+ * `data`. */
+pfdd_status pfdd_fft_device_noalloc(void *data, int n1, int n2, int n3, int batch, int precision, int sign,
+                                    void *stream);
 
 const char *pfdd_status_string(int status);
 

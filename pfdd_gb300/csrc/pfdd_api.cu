@@ -161,81 +161,6 @@ using namespace pfdd;
 
 namespace {
 
-constexpr int kThreads = 256;
-
-bool pow2_ok(int n) { return n >= 1 && n <= 512 && (n & (n - 1)) == 0; }
-
-int ilog2(long long v) {
-  int l = 0;
-  while ((1LL << l) < v) ++l;
-  return l;
-}
-
-struct Geometry {
-  // z-pass
-  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0;
-  size_t zSmem = 0;
-  // strided passes (y: axis 1, x: axis 0; x only in the FFT-boundary plans)
-  int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1};
-  long long tiles[2] = {1, 1};
-  size_t smem[2] = {0, 0};
-  // fused x-pass
-  int xLgT = 0, xPitch = 1, xThreads = 256;
-  long long xTiles = 1;
-  size_t xSmem = 0;
-};
-
-static int line_pitch(int L) { return L >= 8 ? L + L / 8 : L; }  // pad8 layout of a contiguous line
-
-// ns = 0: no fused x-pass (FFT-boundary plans).  bsize: bytes of a B(k) value.
-Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize) {
-  Geometry g;
-  const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
-  const long long lines = (long long)n1 * n2;
-  int TL = std::max(1, kThreads / team3);
-  while ((long long)TL > lines) TL >>= 1;
-  g.zTL = TL;
-  g.zThreads = TL * team3;
-  g.zPitch = line_pitch(L3);
-  g.zNparts = (int)(lines / TL);
-  // twiddles + padded S lines (16-byte aligned) + FP64 xi tile
-  g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
-  g.lgL3 = ilog2(L3);
-  const int Ls[2] = {n2, n1};
-  const long long inner[2] = {(long long)n3, (long long)n2 * n3};
-  for (int ax = 0; ax < 2; ++ax) {
-    const int L = Ls[ax], E = std::min(8, L), team = L / E;
-    int TI = std::max(1, kThreads / team);
-    while ((long long)TI > inner[ax]) TI >>= 1;
-    g.lgTI[ax] = ilog2(TI);
-    g.threads[ax] = TI * team;
-    g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
-    g.tiles[ax] = inner[ax] / TI;
-    g.smem[ax] = ((size_t)L + (size_t)L * g.pitch[ax]) * vsize;
-  }
-  if (ns > 0) {
-    // x-pass tile: T consecutive inner indices of all N1 x and all ns fields plus
-    // the tile's B(k), sized for two CTAs per SM (<= 110 KB), T <= 32
-    const long long innerx = (long long)n2 * n3;
-    g.xPitch = line_pitch(n1);
-    int lgT = 5;
-    while (lgT > 0 && ((1LL << lgT) > innerx ||
-                       x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize) > 110 * 1024))
-      --lgT;
-    g.xLgT = lgT;
-    g.xTiles = innerx >> lgT;
-    g.xSmem = x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize);
-    const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
-    const int unit = std::max(32, team);
-    const int cap = vsize == sizeof(double2) ? 256 : 384;  // x_fused_kernel launch bounds
-    int thr = std::min(cap, std::max(npt, lines * team));
-    thr = (thr + unit - 1) / unit * unit;
-    g.xThreads = std::min(thr, cap / unit * unit);
-  }
-  return g;
-}
-
-
 // kernels of a step, for the optional per-kernel event timing
 enum KId { K_Z_PROLOGUE, K_Z_STEP, K_FFT_Y_FWD, K_FFT_X_FWD, K_CONTRACT, K_FFT_X_INV, K_FFT_Y_INV, K_GAMMA,
            K_X_FUSED, K_PLANE, K_PLANE_PROLOGUE, K_COUNT };
@@ -350,6 +275,7 @@ extern "C" const char *pfdd_status_string(int s) {
     case PFDD_ETIMEOUT: return "device wait timed out";
     case PFDD_ENONFINITE: return "state became non-finite";
     case PFDD_ENOTREADY: return "input not set";
+    case PFDD_ELIMIT: return "size beyond a fixed capacity";
     default: return "unknown status";
   }
 }

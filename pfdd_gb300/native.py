@@ -18,7 +18,7 @@ from . import workloads
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpfdd_gb300.so"
 
-PFDD_OK, PFDD_EINVAL, PFDD_ENOMEM, PFDD_ECUDA, PFDD_ETIMEOUT, PFDD_ENONFINITE, PFDD_ENOTREADY = range(7)
+PFDD_OK, PFDD_EINVAL, PFDD_ENOMEM, PFDD_ECUDA, PFDD_ETIMEOUT, PFDD_ENONFINITE, PFDD_ENOTREADY, PFDD_ELIMIT = range(8)
 PRECISIONS = {"fp64": 0, "fp32": 1}
 
 # every entry point declared in include/pfdd_gpu.h and include/pfdd_setup.h
@@ -30,6 +30,7 @@ EXPORTS = [
     "pfdd_required_bytes", "pfdd_fft_plan_create", "pfdd_fft_plan_destroy", "pfdd_fft_forward",
     "pfdd_fft_backward", "pfdd_status_string", "pfdd_frec", "pfdd_setfcc", "pfdd_setorient", "pfdd_seteps",
     "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
+    "pfdd_fft_device_noalloc",
 ]
 
 _lib = None
@@ -81,6 +82,7 @@ def load():
     L.pfdd_fft_plan_destroy.restype = None
     L.pfdd_fft_forward.argtypes = [vp, vp, i, i]
     L.pfdd_fft_backward.argtypes = [vp, vp, i, i]
+    L.pfdd_fft_device_noalloc.argtypes = [vp, i, i, i, i, i, i, vp]
     L.pfdd_status_string.argtypes = [i]
     L.pfdd_status_string.restype = C.c_char_p
     L.pfdd_frec.argtypes = [i, d, dp]
