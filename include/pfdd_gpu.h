@@ -49,8 +49,13 @@ typedef enum {
 } pfdd_status;
 
 typedef enum {
-  PFDD_FP64 = 0,      /* plain form: FFTs, contraction and update in FP64 */
-  PFDD_FFT_FP32 = 1   /* precision form: complex64 FFTs + FP32 contraction, FP64 state/sums */
+  PFDD_FP64 = 0,          /* plain form: FFTs, contraction and update in FP64 */
+  PFDD_FFT_FP32 = 1,      /* precision form: complex64 FFTs + FP32 contraction with B(k) built in
+                             FP64 and stored rounded to FP32; FP64 state and sums */
+  PFDD_FFT_FP32_BFLY = 2  /* as PFDD_FFT_FP32, but the x-pass evaluates B(k) in FP32 registers
+                             from the same closed form instead of reading a stored table (no B
+                             memory, 4 bytes x ns(ns+1)/2 less traffic per point and step); needs
+                             pfdd_build_B and 32 <= N1 <= 256.  Whole-step contexts only. */
 } pfdd_precision;
 
 typedef struct pfdd_ctx pfdd_ctx;

@@ -191,7 +191,7 @@ struct pfdd_ctx {
   double *tau = nullptr, *part = nullptr, *gam_a = nullptr, *gam = nullptr;
   double *tau_field = nullptr, *dslip_dev = nullptr;
   uint8_t *active = nullptr;
-  int *flag = nullptr;
+  int *flag = nullptr, *errflag = nullptr, *h_errflag = nullptr;
   void *tw[3] = {nullptr, nullptr, nullptr};
   double *h_gam_a = nullptr, *h_gam = nullptr, *h_tau = nullptr;
   std::vector<uint8_t> h_active;
@@ -200,6 +200,7 @@ struct pfdd_ctx {
   int kchunk = 1;
   Geometry g;
   BLayout bl{};
+  BFlyParams bf{};
   long long launches = 0;
   KTiming tm;
   std::string err;
@@ -255,7 +256,11 @@ static void t_end(pfdd_ctx *c, int id) {
 }
 
 static size_t vsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double2) : sizeof(float2); }
-static size_t bsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double) : sizeof(float); }
+// bytes of a stored B(k) value; 0: the x-pass evaluates B(k) itself
+static size_t bsize_of(int prec) {
+  return prec == PFDD_FP64 ? sizeof(double) : (prec == PFDD_FFT_FP32 ? sizeof(float) : 0);
+}
+static bool prec_ok(int prec) { return prec == PFDD_FP64 || prec == PFDD_FFT_FP32 || prec == PFDD_FFT_FP32_BFLY; }
 
 extern "C" size_t pfdd_required_bytes(int n1, int n2, int n3, int ns, int nrep, int precision) {
   const size_t N = (size_t)n1 * n2 * n3, P = (size_t)ns * (ns + 1) / 2, RF = (size_t)nrep * ns;
@@ -300,9 +305,9 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
                                            int device) {
   if (!out) return PFDD_EINVAL;
   *out = nullptr;
-  if (!pow2_ok(n1) || !pow2_ok(n2) || !pow2_ok(n3) || ns < 1 || ns > 12 || nrep < 1 ||
-      (precision != PFDD_FP64 && precision != PFDD_FFT_FP32))
+  if (!pow2_ok(n1) || !pow2_ok(n2) || !pow2_ok(n3) || ns < 1 || ns > 12 || nrep < 1 || !prec_ok(precision))
     return PFDD_EINVAL;
+  if (precision == PFDD_FFT_FP32_BFLY && (n1 < 32 || n1 > 256)) return PFDD_EINVAL;
   pfdd_ctx *c = new pfdd_ctx();
   *out = c;
   c->n[0] = n1; c->n[1] = n2; c->n[2] = n3;
@@ -315,10 +320,13 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
   CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
   CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
-  CK(c, cudaMalloc(&c->B, P * N * bsize_of(precision)));
+  if (bsize_of(precision)) CK(c, cudaMalloc(&c->B, P * N * bsize_of(precision)));
   CK(c, cudaMalloc(&c->active, nrep));
   CK(c, cudaMalloc(&c->dslip_dev, kMaxNs * sizeof(double)));
   CK(c, cudaMalloc(&c->flag, sizeof(int)));
+  CK(c, cudaMalloc(&c->errflag, sizeof(int)));
+  CK(c, cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st));
+  CK(c, cudaMallocHost(&c->h_errflag, sizeof(int)));
   // partial sums for a chunk of steps, bounded to ~32 MB
   const size_t per_step = RF * (size_t)c->g.zNparts;
   c->kchunk = (int)std::max<size_t>(1, std::min<size_t>(1024, (4u << 20) / std::max<size_t>(per_step, 1)));
@@ -345,7 +353,8 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   cudaSetDevice(c->dev);
   if (c->st) cudaStreamSynchronize(c->st);
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
-                c->active, c->flag, c->tw[0], c->tw[1], c->tw[2]};
+                c->active, c->flag, c->errflag, c->tw[0], c->tw[1], c->tw[2]};
+  if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
   for (void *p : dp)
     if (p) cudaFree(p);
@@ -358,6 +367,8 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
 
 extern "C" pfdd_status pfdd_set_B(pfdd_ctx *c, const double *B) {
   if (!c || !B) return fail(c, PFDD_EINVAL, "pfdd_set_B: null argument");
+  if (c->prec == PFDD_FFT_FP32_BFLY)
+    return fail(c, PFDD_EINVAL, "pfdd_set_B: this context evaluates B(k) itself; use pfdd_build_B");
   CK(c, cudaSetDevice(c->dev));
   const size_t full = (size_t)c->ns * c->ns * c->N * sizeof(double);
   double *tmp = nullptr;
@@ -378,6 +389,7 @@ extern "C" pfdd_status pfdd_set_B(pfdd_ctx *c, const double *B) {
 extern "C" pfdd_status pfdd_get_B(pfdd_ctx *c, double *B) {
   if (!c || !B) return fail(c, PFDD_EINVAL, "pfdd_get_B: null argument");
   if (!c->hasB) return fail(c, PFDD_ENOTREADY, "pfdd_get_B: B(k) not set");
+  if (c->prec == PFDD_FFT_FP32_BFLY) return fail(c, PFDD_EINVAL, "pfdd_get_B: no stored B(k) in this context");
   CK(c, cudaSetDevice(c->dev));
   const size_t full = (size_t)c->ns * c->ns * c->N * sizeof(double);
   double *tmp = nullptr;
@@ -425,6 +437,20 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
         for (int j = 0; j < 3; ++j) s += eps[(a * 3 + i) * 3 + j] * hp.sig[b][i][j];
       hp.E[a][b] = s;
     }
+  if (c->prec == PFDD_FFT_FP32_BFLY) {  // the x-pass evaluates the same closed form in FP32
+    BFlyParams &bf = c->bf;
+    bf.n2 = c->n[1]; bf.n3 = c->n[2]; bf.lgN3 = ilog2(c->n[2]);
+    bf.d[0] = (float)d1; bf.d[1] = (float)d2; bf.d[2] = (float)d3;
+    bf.mu = (float)hp.mu; bf.ll = (float)hp.ll; bf.mup = (float)hp.mup; bf.mu_inv = (float)hp.mu_inv;
+    int q = 0;
+    for (int a = 0; a < c->ns; ++a) {
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) bf.sig[a][i][j] = (float)hp.sig[a][i][j];
+      for (int b = a; b < c->ns; ++b, ++q) bf.E[q] = (float)hp.E[a][b];
+    }
+    c->hasB = true;
+    return PFDD_OK;
+  }
   BBuildParams *dp = nullptr;
   CK(c, cudaMalloc(&dp, sizeof hp));
   cudaError_t e = cudaMemcpyAsync(dp, &hp, sizeof hp, cudaMemcpyHostToDevice, c->st);
@@ -568,9 +594,13 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   xp.L = c->n[0]; xp.lgL = ilog2(c->n[0]); xp.lgT = c->g.xLgT; xp.pitch = c->g.xPitch; xp.R = c->nrep;
   const unsigned blocks = (unsigned)(c->nrep * c->g.xTiles);
   t_begin(c);
-  cudaError_t e = std::is_same<T, float>::value
-                      ? launch_x_fused_f32(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
-                      : launch_x_fused_f64(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp);
+  xp.bf = c->bf;
+  xp.err = c->errflag;
+  cudaError_t e = c->prec == PFDD_FFT_FP32_BFLY
+                      ? launch_x_fused_f32_bfly(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
+                      : (std::is_same<T, float>::value
+                             ? launch_x_fused_f32(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
+                             : launch_x_fused_f64(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp));
   t_end(c, K_X_FUSED);
   return e;
 }
@@ -580,7 +610,7 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
   ZParams zp;
   std::memset(&zp, 0, sizeof zp);
   zp.S = c->S; zp.xi = c->xi; zp.bc = c->anyBc ? c->bc : nullptr; zp.tau = c->tau; zp.tau_field = c->tau_field;
-  zp.dslip = c->dslip_dev; zp.part = c->part;
+  zp.dslip = c->dslip_dev; zp.part = c->part; zp.err = c->errflag;
   zp.active = c->active;
   zp.tw = c->tw[2];
   zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
@@ -623,7 +653,15 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(c->h_gam_a, c->gam_a, (size_t)ks * RF * sizeof(double), cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaMemcpyAsync(c->h_gam, c->gam, (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(c, cudaMemcpyAsync(c->h_errflag, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
+    if (*c->h_errflag) {
+      CK(c, cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st));
+      CK(c, cudaStreamSynchronize(c->st));
+      c->specValid = false;
+      return fail(c, PFDD_ETIMEOUT, "pfdd_step: a bounded device wait for a bulk copy ran out within steps %d..%d",
+                  s0, s0 + ks - 1);
+    }
     bool finite = true;
     for (int q = 0; q < nt; ++q)
       if (c->h_active[q % c->nrep] && !std::isfinite(c->h_gam[q])) finite = false;

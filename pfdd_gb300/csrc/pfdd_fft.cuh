@@ -75,10 +75,6 @@ template <int S, typename V> __device__ __forceinline__ void dft8(V *x) {
   x[3] = cadd(e3, o3); x[7] = csub(e3, o3);
 }
 
-// Padded position of element l in a contiguous line: one pad slot per 8
-// elements, so the stride-8 writes of the first radix-8 stage hit distinct banks.
-__device__ __forceinline__ int pad8(int l) { return l + (l >> 3); }
-
 // One Stockham stage of radix R = 2^lgR for a team thread th holding
 // v[m] = line[th + m*L/8].  Ns = 2^lgNs radices already applied.
 template <int S, int R, typename V, typename Addr>
@@ -111,7 +107,10 @@ __device__ __forceinline__ void stockham_stage(V *v, int th, int lgL, int lgNs, 
 
 // Full transform of the team's line, data in shared memory in natural order
 // before and after; sm(l) addresses element l.  tw: forward twiddles of
-// length L (shared memory).  Every thread of the block must call it.
+// length L (shared memory).  Every thread of the block must call it (the
+// stages end with block barriers); the caller synchronises the block before
+// the first stage.  Kernels map consecutive lanes to different lines (the
+// twiddle loads of a warp are then broadcasts) and give lines an odd pitch.
 // LG >= 0 fixes log2(L) at compile time (stage loop unrolled, all index
 // arithmetic folded); LG < 0 takes it from lgL at run time.
 template <int S, int LG, typename V, typename Addr>
@@ -150,7 +149,6 @@ __device__ __forceinline__ void line_fft(int th, int lgL_rt, const V *tw, Addr s
         *sm(0) = a0; *sm(1) = a1;
       }
     }
-    __syncthreads();
   }
 }
 

@@ -17,6 +17,7 @@
 #pragma once
 #include "pfdd_convert.cuh"
 #include "pfdd_fft.cuh"
+#include "pfdd_tma.cuh"
 
 namespace pfdd {
 
@@ -39,6 +40,7 @@ struct ZParams {
   double *part;             // [step][R*ns][nparts]
   const uint8_t *active;    // [R] or null
   const void *tw;           // forward twiddles of length L
+  int *err;                 // set when a bounded wait times out (may be null)
   long long N, lines_per_field;
   int step, L, lgL, ns, R, TL, nparts, flags, pitch;
   double inv_n, uq2;
@@ -129,7 +131,7 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *red) 
 }
 
 // z-pass: TL contiguous lines of length L (one field), see ZFlags.
-// Shared memory: twiddles [L] | S lines [TL][pitch] (padded) | xi tile
+// Shared memory: twiddles [L] | S lines [TL][pitch] (odd pitch) | xi tile
 // [TL*L] double2 (update only).  The S lines and the xi tile are fetched with
 // cp.async in two completion groups so the xi fetch overlaps the inverse FFT.
 template <typename T, int LG>
@@ -152,8 +154,13 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   V *S = reinterpret_cast<V *>(p.S);
   const bool upd = (p.flags & Z_UPDATE) != 0;
-  auto sidx = [&](int e) { return (e >> lgL) * P + pad8(e & (L - 1)); };
+  auto sidx = [&](int e) { return (e >> lgL) * P + (e & (L - 1)); };
 
+  __shared__ __align__(8) uint64_t xbar;  // completion of the FP64 state tile
+  if (upd && tid == 0) {  // the state tile is one contiguous block: TMA bulk copies
+    mbar_init(&xbar, 1);
+    bulk_load(xs, p.xi + e0, (unsigned)nel * 16u, &xbar);
+  }
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   if (p.flags & Z_SRC_XI) {
     for (int e = tid; e < nel; e += nthr) sm[sidx(e)] = from_xi<V>(p.xi[e0 + e]);
@@ -161,20 +168,16 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
     for (int e = tid; e < nel; e += nthr) cp_async_elem(&sm[sidx(e)], &S[e0 + e]);
   }
   cp_async_commit();
-  if (upd) {
-    for (int e = tid; e < nel; e += nthr) cp_async16(&xs[e], &p.xi[e0 + e]);
-  }
-  cp_async_commit();
-  cp_async_wait<1>();
+  cp_async_wait<0>();
   __syncthreads();
-  const int t = tid / team, th = tid - t * team;
-  const bool act = t < TL;
-  auto line = [&](int l) { return &sm[t * P + pad8(l)]; };
+  const int t = tid % TL, th = tid / TL;  // consecutive lanes on consecutive lines
+  const bool act = th < team;
+  auto line = [&](int l) { return &sm[t * P + l]; };
   if (p.flags & Z_INV) line_fft<+1, LG>(th, lgL, tws, line, act);
 
   if (upd) {
-    cp_async_wait<0>();
-    __syncthreads();
+    mbar_wait(&xbar, 0, p.err);
+    __syncthreads();  // the update reads elements of other teams' lines
     const UpdCoef<T> k(p, a);
     const double tv = p.tau[((long long)p.step * p.R + r) * p.ns + a];
     const auto ctau0 = k.tau(tv);
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
 
   if (p.flags & Z_FWD) line_fft<-1, LG>(th, lgL, tws, line, act);
   if (p.flags & Z_STORE) {
-    if (L < 8) __syncthreads();
+    __syncthreads();
     for (int e = tid; e < nel; e += nthr) S[e0 + e] = sm[sidx(e)];
   }
 }
@@ -277,9 +280,10 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
   cp_async_wait<0>();
   __syncthreads();
   const int E = L >= 8 ? 8 : L, team = L / E;
-  const int t = tid & (TI - 1), th = tid >> lgTI;
+  const int t = tid & (TI - 1), th = tid >> lgTI;  // consecutive lanes on consecutive lines
   const bool act = th < team;
   line_fft<S, LG>(th, lgL, tws, [&](int l) { return &sm[l * pitch + t]; }, act);
+  __syncthreads();
   for (int e = tid; e < nel; e += nthr) {
     const int l = e >> lgTI, tt = e & (TI - 1);
     base[(long long)l * inner + tt] = sm[l * pitch + tt];
@@ -299,6 +303,15 @@ __host__ __device__ __forceinline__ long long b_index(const BLayout &bl, int p, 
   return (tile * bl.P + p) * ((long long)bl.L << bl.lgT) + t * bl.L + x;
 }
 
+// Constants of the closed-form B(k) for the x-pass that evaluates B in FP32
+// registers instead of streaming a stored table (see x_fused_kernel, BFLY).
+struct BFlyParams {
+  int n2, n3, lgN3;
+  float d[3], mu, ll, mup, mu_inv;
+  float sig[kMaxNs][3][3];                 // sigma_a = C : eps_a
+  float E[kMaxNs * (kMaxNs + 1) / 2];      // eps_a : C : eps_b, packed pairs a <= b
+};
+
 struct XParams {
   void *S;
   const void *B;
@@ -306,7 +319,17 @@ struct XParams {
   const void *tw;          // x-axis forward twiddles (length L = N1)
   long long inner, tiles;  // inner = N2*N3, tiles = inner / T per field row
   int L, lgL, lgT, pitch, R;
+  int *err;                // set when a bounded wait times out (may be null)
+  BFlyParams bf;
 };
+
+// frec (F:2683-2754) in FP32: exact for power-of-two n and unit spacing
+__device__ __forceinline__ float frec_f(int i, int n, float d) {
+  float v = 0.0f;
+  if (i >= 1 && i < n / 2) v = (float)i / (float)n / d;
+  if (i >= n / 2) v = ((float)i - (float)n) / (float)n / d;
+  return v;
+}
 
 // Shared-memory bytes of the fused x-pass for a tile of T = 2^lgT.
 __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, int pitch, size_t vsize,
@@ -319,13 +342,16 @@ __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, 
 // Fused x-pass on a tile of T consecutive inner indices, all N1 x-values and
 // all NS fields of one replica: forward FFT along x, k-space contraction
 // S[a](k) <- sum_b B_ab(k) S[b](k) (F:4609-4629, b ascending), inverse FFT
-// along x.  Shared memory: twiddles [L] | tile [a][t][x] (x contiguous,
-// padded) | B tile [P][T*L].  The S tile and the B tile arrive by cp.async in
+// along x.  Shared memory: twiddles [L] | tile [a][t][x] (x contiguous, odd
+// line pitch) | B tile [P][T*L].  The S tile and the B tile arrive by cp.async in
 // two groups, so the B fetch overlaps the forward FFT.  One point per thread
 // in the contraction; IN_REGS keeps its NS inputs in registers (FP32, up to
 // 384 threads); FP64 reads them from shared memory and runs at most 256 threads.
-template <typename T, int NS, bool IN_REGS, int LG>
-__global__ void __launch_bounds__(IN_REGS ? 384 : 256, 2) x_fused_kernel(XParams p) {
+// BFLY (FP32 only): B_ab(k) = (E_ab - u_a . t_b) / mu with t_b = sigma_b f and
+// u_a = G(f) t_a, the closed form of Bmatrix (F:328-412), evaluated per point in
+// FP32 registers; no B table is read (the x-pass then moves only the fields).
+template <typename T, int NS, bool IN_REGS, int LG, bool BFLY>
+__global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_kernel(XParams p) {
   using V = typename cpx<T>::t;
   constexpr int P = NS * (NS + 1) / 2;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -343,7 +369,7 @@ __global__ void __launch_bounds__(IN_REGS ? 384 : 256, 2) x_fused_kernel(XParams
   const T *Bt = reinterpret_cast<const T *>(p.B) + tile * P * (long long)npt;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nel = (NS * L) << lgT;
-  auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + pad8(x); };
+  auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + x; };
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   // S tile: e -> (a, x, t) with t fastest (contiguous in memory)
   for (int e = tid; e < nel; e += nthr) {
@@ -351,25 +377,27 @@ __global__ void __launch_bounds__(IN_REGS ? 384 : 256, 2) x_fused_kernel(XParams
     cp_async_elem(&sm[sidx(a, t, x)], &S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t]);
   }
   cp_async_commit();
-  // B tile: one contiguous block of P * npt values
-  const int bbytes = P * npt * (int)sizeof(T);
-  if ((bbytes & 15) == 0) {
-    for (int i = tid; i < (bbytes >> 4); i += nthr)
-      cp_async16(reinterpret_cast<char *>(Bs) + 16 * i, reinterpret_cast<const char *>(Bt) + 16 * i);
-  } else {
-    for (int i = tid; i < P * npt; i += nthr) Bs[i] = Bt[i];
+  // B tile: one contiguous block of P * npt values, TMA bulk copies issued by
+  // one thread so it streams in during the forward FFT
+  __shared__ __align__(8) uint64_t bbar;
+  const int bbytes = BFLY ? 0 : P * npt * (int)sizeof(T);
+  const bool bulk = !BFLY && (bbytes & 15) == 0;
+  if (bulk && tid == 0) {
+    mbar_init(&bbar, 1);
+    bulk_load(Bs, Bt, (unsigned)bbytes, &bbar);
   }
-  cp_async_commit();
-  cp_async_wait<1>();
+  if (!BFLY && !bulk)
+    for (int i = tid; i < P * npt; i += nthr) Bs[i] = Bt[i];
+  cp_async_wait<0>();
   __syncthreads();
   const int E = L >= 8 ? 8 : L, team = L / E, teams = nthr / team;
   const int lines = NS << lgT;
-  const int my_team = tid / team, th = tid - my_team * team;
+  const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
   for (int l0 = 0; l0 < lines; l0 += teams) {
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
     line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
   }
-  cp_async_wait<0>();
+  if (bulk) mbar_wait(&bbar, 0, p.err);
   __syncthreads();
   for (int q = tid; q < npt; q += nthr) {
     const int t = q >> lgL, x = q & (L - 1);
@@ -380,13 +408,55 @@ __global__ void __launch_bounds__(IN_REGS ? 384 : 256, 2) x_fused_kernel(XParams
       out[a] = V{0, 0};
       if (IN_REGS) in[a] = sm[sidx(a, t, x)];
     }
+    // closed-form B(k) of this point (BFLY): frequencies, G(f), t_b = sigma_b f
+    float G00 = 0, G01 = 0, G02 = 0, G11 = 0, G12 = 0, G22 = 0, tv[BFLY ? NS : 1][3];
+    bool nonzero = true;
+    if (BFLY) {
+      const BFlyParams &bf = p.bf;
+      const long long c = c0 + t;
+      const int j = (int)(c >> bf.lgN3), k = (int)(c & (bf.n3 - 1));
+      const float f0 = frec_f(x, L, bf.d[0]), f1 = frec_f(j, bf.n2, bf.d[1]), f2 = frec_f(k, bf.n3, bf.d[2]);
+      const float ff = f0 * f0 + f1 * f1 + f2 * f2;
+      nonzero = ff > 0.0f;
+      if (nonzero) {
+        const float inv = 1.0f / ff;
+        const float z0 = f0 * f0 * inv, z1 = f1 * f1 * inv, z2 = f2 * f2 * inv;
+        const float d0 = bf.mu + bf.mup * z0, d1 = bf.mu + bf.mup * z1, d2 = bf.mu + bf.mup * z2;
+        const float i0 = 1.0f / d0, i1 = 1.0f / d1, i2 = 1.0f / d2;
+        const float kk = 1.0f + (bf.mu + bf.ll) * (i0 * z0 + i1 * z1 + i2 * z2);
+        const float cc = (bf.mu + bf.ll) / kk * inv;
+        G00 = inv * (i0 - f0 * f0 * i0 * i0 * cc);
+        G11 = inv * (i1 - f1 * f1 * i1 * i1 * cc);
+        G22 = inv * (i2 - f2 * f2 * i2 * i2 * cc);
+        G01 = -inv * f0 * f1 * i0 * i1 * cc;
+        G02 = -inv * f0 * f2 * i0 * i2 * cc;
+        G12 = -inv * f1 * f2 * i1 * i2 * cc;
+#pragma unroll
+        for (int b = 0; b < (BFLY ? NS : 1); ++b)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) tv[b][i] = bf.sig[b][i][0] * f0 + bf.sig[b][i][1] * f1 + bf.sig[b][i][2] * f2;
+      }
+    }
     int pidx = 0;
 #pragma unroll
     for (int a = 0; a < NS; ++a) {
       const V ina = IN_REGS ? in[a] : sm[sidx(a, t, x)];
+      float ua0 = 0, ua1 = 0, ua2 = 0;
+      if (BFLY) {
+        const int aa = BFLY ? a : 0;
+        ua0 = G00 * tv[aa][0] + G01 * tv[aa][1] + G02 * tv[aa][2];
+        ua1 = G01 * tv[aa][0] + G11 * tv[aa][1] + G12 * tv[aa][2];
+        ua2 = G02 * tv[aa][0] + G12 * tv[aa][1] + G22 * tv[aa][2];
+      }
 #pragma unroll
       for (int b = a; b < NS; ++b, ++pidx) {
-        const T v = Bs[pidx * npt + q];
+        T v;
+        if (BFLY) {
+          const int bb = BFLY ? b : 0;
+          v = nonzero ? (p.bf.E[pidx] - (ua0 * tv[bb][0] + ua1 * tv[bb][1] + ua2 * tv[bb][2])) * p.bf.mu_inv : (T)0;
+        } else {
+          v = Bs[pidx * npt + q];
+        }
         const V inb = IN_REGS ? in[b] : sm[sidx(b, t, x)];
         out[a].x += inb.x * v;
         out[a].y += inb.y * v;
@@ -404,7 +474,7 @@ __global__ void __launch_bounds__(IN_REGS ? 384 : 256, 2) x_fused_kernel(XParams
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
     line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
   }
-  if (L < 8) __syncthreads();
+  __syncthreads();
   for (int e = tid; e < nel; e += nthr) {
     const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
     S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t] = sm[sidx(a, t, x)];

@@ -21,6 +21,9 @@ cudaError_t launch_strided(int prec, int sign, int lgL, unsigned blocks, int thr
 // fused x-pass (x-forward FFT, contraction, x-inverse FFT) for ns in [1, 12]
 cudaError_t launch_x_fused_f32(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p);
 cudaError_t launch_x_fused_f64(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p);
+// FP32 x-pass evaluating B(k) in registers, N1 in [32, 256]
+cudaError_t launch_x_fused_f32_bfly(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st,
+                                    const XParams &p);
 
 // Launch geometry of the z-pass, the strided passes and the fused x-pass for one
 // grid (ns = 0: FFT-boundary plans without the x-pass).  Sizes: powers of two <= 512.
@@ -48,9 +51,10 @@ struct Geometry {
   size_t xSmem = 0;
 };
 
-inline int line_pitch(int L) { return L >= 8 ? L + L / 8 : L; }  // pad8 layout of a contiguous line
+inline int line_pitch(int L) { return L + 1; }  // odd pitch: lanes on different lines hit different banks
 
-// ns = 0: no fused x-pass (FFT-boundary plans).  bsize: bytes of a B(k) value.
+// ns = 0: no fused x-pass (FFT-boundary plans).  bsize: bytes of a stored B(k)
+// value, 0 when the x-pass evaluates B(k) itself.
 inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize) {
   Geometry g;
   const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
@@ -90,7 +94,7 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
     g.xSmem = x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize);
     const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
     const int unit = std::max(32, team);
-    const int cap = vsize == sizeof(double2) ? 256 : 384;  // x_fused_kernel launch bounds
+    const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
     int thr = std::min(cap, std::max(npt, lines * team));
     thr = (thr + unit - 1) / unit * unit;
     g.xThreads = std::min(thr, cap / unit * unit);

@@ -19,7 +19,7 @@ from . import workloads
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpfdd_gb300.so"
 
 PFDD_OK, PFDD_EINVAL, PFDD_ENOMEM, PFDD_ECUDA, PFDD_ETIMEOUT, PFDD_ENONFINITE, PFDD_ENOTREADY, PFDD_ELIMIT = range(8)
-PRECISIONS = {"fp64": 0, "fp32": 1}
+PRECISIONS = {"fp64": 0, "fp32": 1, "fp32_bfly": 2}
 
 # every entry point declared in include/pfdd_gpu.h and include/pfdd_setup.h
 EXPORTS = [

@@ -201,3 +201,35 @@ def test_missing_inputs_are_reported(native_lib):
         s.step(np.zeros((1, 3)))
     assert ei.value.status == native.PFDD_ENOTREADY
     s.close()
+
+
+def test_fp32_bfly_form_error_vs_fp64_oracle(native_lib):
+    """FP32 form with B(k) evaluated in the x-pass (no stored table): same error class
+    as the stored-table FP32 form against the FP64 oracle, and close to it."""
+    spec = workloads.config0()
+    xo, go, _ = oracle.solve(spec)
+    xb, gb, _, _ = run_gpu(spec, "fp32_bfly")
+    xs, gs, _, _ = run_gpu(spec, "fp32")
+    assert rel(gb, go) <= FP32_GAMMA_RTOL
+    assert np.max(np.abs(xb - xo)) <= 1e-5
+    assert rel(gb, gs) <= 1e-6
+
+
+def test_fp32_bfly_noncubic_and_batched(native_lib):
+    base = workloads.SolveSpec(n=(32, 8, 16), ns=12, steps=8, sigma_max=0.05,
+                               loops=workloads.random_loops((32, 8, 16), 3, 2.0, 5.0, 12, seed=21))
+    specs = [workloads.SolveSpec(**{**base.__dict__, "noise_seed": 60 + r, "sigma_max": 0.02 * (r + 1)})
+             for r in range(2)]
+    s = native.solver_for(specs[0], "fp32_bfly", nrep=2)
+    s.set_state(np.stack([workloads.initial_state(sp)[0] for sp in specs]),
+                np.stack([workloads.initial_state(sp)[1] for sp in specs]))
+    g, _ = s.step(np.stack([native.spec_tau(sp) for sp in specs], axis=1))
+    xb = s.get_state()
+    with pytest.raises(native.PFDDError):
+        s.get_B()
+    s.close()
+    for r, sp in enumerate(specs):
+        xr, gr, _, _ = run_gpu(sp, "fp32_bfly")
+        np.testing.assert_array_equal(xb[r], xr)
+        xo, go, _ = oracle.solve(sp)
+        assert rel(gr, go) <= FP32_GAMMA_RTOL
