@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=0, help="timed steps of the FP64 form (default: steps/4)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving leg, print its JSON")
+    ap.add_argument("--serve-scale", type=float, default=0.1,
+                    help="step-count scale of the 96-request serving mix (0 skips the serving leg)")
     return ap.parse_args()
 
 
@@ -268,6 +271,113 @@ def cpu_baseline_port(spec, B, K_sample=2):
                       f"(FP64 restatement, {oracle.nthreads()} threads)"}
 
 
+def _class_step_ms(native, spec, xi, prec, dev, W=3, K=10):
+    """Device time of one step of a lone solve of this class (its own context)."""
+    import torch
+    s = native.solver_for(spec, prec, device=dev)
+    s.set_state(xi)
+    tau = np.repeat(native.spec_tau(spec)[-1:], W + K, axis=0)
+    s.step(tau[:W])
+    stream = torch.cuda.ExternalStream(s.stream, device=f"cuda:{dev}")
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s.step(tau[W:])
+    e1.record(stream)
+    e1.synchronize()
+    s.close()
+    return e0.elapsed_time(e1) / K
+
+
+def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_steps=25):
+    """The 96-request uneven serving mix through the native server (pfdd_server_*),
+    FP32-FFT form: once with every request queued at t=0 (saturated throughput),
+    once with Poisson arrivals at `load` x that throughput (time-to-solution)."""
+    from pfdd_gb300 import serve
+    reqs = workloads.config4_requests(scale_steps=scale)
+    # one seeded initial state per (grid, systems) class, reused by the class's
+    # requests: a step's cost does not depend on the values of xi
+    inputs = {}
+    for sp in reqs:
+        key = (sp.n, sp.ns)
+        if key not in inputs:
+            inputs[key] = native._interleave(workloads.initial_state(sp)[0].reshape(sp.ns, -1))
+    eps = {ns: native.fcc_eps(ns) for ns in {sp.ns for sp in reqs}}
+
+    def submit(srv, sp):
+        sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = sp.sigma_max
+        tmax = native.resolved_shear(eps[sp.ns], sig)
+        C44, C12 = sp.mu, sp.lam
+        return srv.submit_raw(sp.n, sp.ns, sp.steps, 2.0 * C44 + C12, C12, C44, eps[sp.ns], tmax,
+                              inputs[(sp.n, sp.ns)], None, cd2=sp.cd2, asf=sp.asf, dslip=sp.dslip,
+                              want_xi=False)
+
+    # lone-solve step times per class: the one-at-a-time baselines
+    solo = {}
+    for key, xi in inputs.items():
+        sp = next(r for r in reqs if (r.n, r.ns) == key)
+        z = xi[..., 0] + 1j * xi[..., 1]
+        solo[key] = {p: _class_step_ms(native, sp, z, p, dev) for p in ("fp32", "fp64")}
+    total_steps = sum(sp.steps for sp in reqs)
+    total_updates = sum(sp.steps * sp.npts * sp.ns for sp in reqs)
+    seq = {p: sum(sp.steps * solo[(sp.n, sp.ns)][p] for sp in reqs) / 1e3 for p in ("fp32", "fp64")}
+
+    trace = os.environ.get("PFDD_SERVER_TRACE_BASE")  # optional per-run scheduling traces
+    if trace:
+        os.environ["PFDD_SERVER_TRACE"] = trace + ".saturated.csv"
+    with serve.Server("fp32", device=dev, max_slots=max_slots, chunk_steps=chunk_steps) as srv:
+        t0 = time.perf_counter()
+        ids = [submit(srv, sp) for sp in reqs]
+        res = [srv.wait(i) for i in ids]
+        t_sat = time.perf_counter() - t0
+        st_sat = srv.stats()
+    sat_lat = np.array([r.latency_s for r in res])
+    rate = load * len(reqs) / t_sat
+    gaps = np.random.Generator(np.random.PCG64(np.random.SeedSequence([4, 3]))).exponential(1.0 / rate, len(reqs))
+    arrive = np.cumsum(gaps) - gaps[0]
+    if trace:
+        os.environ["PFDD_SERVER_TRACE"] = trace + ".poisson.csv"
+    with serve.Server("fp32", device=dev, max_slots=max_slots, chunk_steps=chunk_steps) as srv:
+        t0 = time.perf_counter()
+        ids = []
+        for sp, ta in zip(reqs, arrive):
+            dt = t0 + ta - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(submit(srv, sp))
+        res = [srv.wait(i) for i in ids]
+        t_poi = time.perf_counter() - t0
+        st_poi = srv.stats()
+    lat = np.array([r.latency_s for r in res])
+    svc = np.array([sp.steps * solo[(sp.n, sp.ns)]["fp32"] / 1e3 for sp in reqs])
+    return {
+        "workload": f"96 requests, grids {{32,64,128,256}}^3 p={{.4,.3,.2,.1}}, NS in {{3,12}}, 1-8 loops, "
+                    f"sigma_max U(0.01,0.06), steps U(200,2000) x {scale}; FP32-FFT form",
+        "requests": len(reqs), "solve_steps": total_steps, "point_system_updates": total_updates,
+        "server": {"max_slots": max_slots, "chunk_steps": chunk_steps, "hbm_budget": "90% of free"},
+        "saturated": {"makespan_s": round(t_sat, 3), "steps_per_s": round(total_steps / t_sat, 1),
+                      "updates_per_s": round(total_updates / t_sat, 1),
+                      "p50_s": round(float(np.percentile(sat_lat, 50)), 4),
+                      "p99_s": round(float(np.percentile(sat_lat, 99)), 4),
+                      "classes_created": st_sat["classes_created"], "peak_bytes": st_sat["peak_bytes"]},
+        "poisson": {"offered_load": load, "arrival_rate_per_s": round(rate, 3), "makespan_s": round(t_poi, 3),
+                    "steps_per_s": round(total_steps / t_poi, 1),
+                    "p50_s": round(float(np.percentile(lat, 50)), 4),
+                    "p99_s": round(float(np.percentile(lat, 99)), 4),
+                    "p50_slowdown": round(float(np.percentile(lat / svc, 50)), 3),
+                    "p99_slowdown": round(float(np.percentile(lat / svc, 99)), 3),
+                    "classes_created": st_poi["classes_created"], "peak_bytes": st_poi["peak_bytes"]},
+        "one_at_a_time": {"fp64_s": round(seq["fp64"], 3), "fp32_s": round(seq["fp32"], 3),
+                          "fp64_steps_per_s": round(total_steps / seq["fp64"], 1),
+                          "fp32_steps_per_s": round(total_steps / seq["fp32"], 1),
+                          "how": "sum over requests of steps x the device step time of a lone solve of "
+                                 "its class (3 warm-up + 10 timed steps per class and form)"},
+        "speedup_vs_fp64_one_at_a_time": round(seq["fp64"] / t_sat, 2),
+        "inputs": "one seeded initial state per (grid, NS) class shared by its requests; each request "
+                  "its own stress ramp and step count",
+    }
+
+
 def run_ours(a):
     dist = Dist(a.gpus)
     import torch
@@ -277,6 +387,10 @@ def run_ours(a):
     dist.barrier()
     dev = dist.local
     torch.cuda.set_device(dev)
+    if a.serve_only:
+        print(json.dumps({"serving": run_serving(native, workloads, dev, a.serve_scale)}), flush=True)
+        dist.close()
+        return
     spec = workloads.config1(n=a.n) if dist.world == 1 else workloads.config1(noise_seed=100 + dist.rank, n=a.n)
     if a.ns != 12:
         spec.ns = a.ns
@@ -326,6 +440,9 @@ def run_ours(a):
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline and r64["B"] is not None:
         cpu = cpu_baseline_port(spec, r64["B"])
+    serving = None
+    if dist.world == 1 and a.serve_scale > 0:
+        serving = run_serving(native, workloads, dev, a.serve_scale)
     launches_per_step = r32["launches"] / K
     out = {
         "metric": METRIC, "value": round(v32, 2), "unit": "steps/s", "n_gpus": dist.world, "steps": K, "warmup": W,
@@ -353,7 +470,7 @@ def run_ours(a):
                   "strain_rel_err_fp32_vs_fp64": strain_err, "strain_err_steps": kk},
         "kernels": kern, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(r32["launches"]), "launches_per_step": round(launches_per_step, 2),
-        "clocks": r32["clocks"],
+        "clocks": r32["clocks"], "serving": serving,
     }
     if dist.rank == 0:
         print(json.dumps(out), flush=True)

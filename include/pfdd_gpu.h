@@ -133,6 +133,13 @@ long long pfdd_last_launch_count(const pfdd_ctx *ctx);
  * work and events against the step. */
 void *pfdd_get_stream(pfdd_ctx *ctx);
 
+/* Recreates the context's stream with a CUDA stream priority (lower = more
+ * urgent; clamped to the device's range, cudaDeviceGetStreamPriorityRange).
+ * No counterpart in the reference (one solve per process); the server gives
+ * classes of small solves more urgent streams so that their short steps are
+ * not queued behind the kernels of large grids. */
+pfdd_status pfdd_set_stream_priority(pfdd_ctx *ctx, int priority);
+
 /* Measurement: with timing on, every kernel launch of the context is bracketed
  * by a CUDA event pair on the context's stream.  pfdd_kernel_stat reports, for
  * kernel kind idx (0 .. until it returns PFDD_EINVAL), its name, the number of

@@ -24,6 +24,7 @@ NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I",
 
 CU_SOURCES = ["pfdd_api.cu", "pfdd_fftpass.cu", "pfdd_xpass_f32.cu", "pfdd_xpass_f64.cu", "pfdd_xpass_f32b.cu", "pfdd_noalloc.cu"]
 C_SOURCES = ["pfdd_setup.c"]
+CXX_SOURCES = ["pfdd_server.cpp"]  # host-only C++ (serving scheduler)
 
 
 def _nvcc() -> str:
@@ -32,7 +33,8 @@ def _nvcc() -> str:
 
 
 def _deps() -> list[Path]:
-    return (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.c")) + list(CSRC.glob("*.h"))
+    return (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.c")) + list(CSRC.glob("*.cpp"))
+            + list(CSRC.glob("*.h"))
             + list((ROOT / "include").glob("*.h")) + list(HOST.glob("*.c")) + [Path(__file__)])
 
 
@@ -59,6 +61,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = objdir / (Path(src).stem + ".o")
         jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-I", str(ROOT / "include"), "-c", str(CSRC / src),
                      "-o", str(obj)])
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include") if "/" in nvcc else "/usr/local/cuda/include"
+    for src in CXX_SOURCES:
+        obj = objdir / (Path(src).stem + ".o")
+        jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-pthread", "-I", str(ROOT / "include"), "-I", cuda_inc,
+                     "-c", str(CSRC / src), "-o", str(obj)])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -69,9 +76,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         list(ex.map(run, jobs))
-    objs = [str(objdir / (Path(s).stem + ".o")) for s in CU_SOURCES + C_SOURCES]
+    objs = [str(objdir / (Path(s).stem + ".o")) for s in CU_SOURCES + C_SOURCES + CXX_SOURCES]
     tmp = LIB.with_suffix(f".so.{os.getpid()}.tmp")
-    run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"])
+    run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart", "-Xcompiler", "-pthread"])
     os.replace(tmp, LIB)
     # C host driver (drop-in for the reference's main loop)
     rtmp = RUNNER.with_suffix(f".{os.getpid()}.tmp")

@@ -703,6 +703,24 @@ extern "C" pfdd_status pfdd_get_replica_state(pfdd_ctx *c, int r, double *xi) {
 
 extern "C" void *pfdd_get_stream(pfdd_ctx *c) { return c ? (void *)c->st : nullptr; }
 
+extern "C" pfdd_status pfdd_set_stream_priority(pfdd_ctx *c, int priority) {
+  if (!c) return PFDD_EINVAL;
+  CK(c, cudaSetDevice(c->dev));
+  int lo = 0, hi = 0;  // least, greatest (numerically lowest) priority
+  CK(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  priority = std::min(lo, std::max(hi, priority));
+  cudaStream_t ns = nullptr;
+  CK(c, cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, priority));
+  cudaError_t e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(ns);
+    CK(c, e);
+  }
+  cudaStreamDestroy(c->st);
+  c->st = ns;
+  return PFDD_OK;
+}
+
 extern "C" pfdd_status pfdd_set_kernel_timing(pfdd_ctx *c, int enable) {
   if (!c) return PFDD_EINVAL;
   c->tm.on = enable != 0;

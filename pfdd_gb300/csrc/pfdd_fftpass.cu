@@ -6,7 +6,7 @@ namespace pfdd {
 
 template <typename T, int LG>
 static cudaError_t zpass_lg(unsigned blocks, int threads, size_t smem, cudaStream_t st, const ZParams &p) {
-  static size_t configured = 48 * 1024;
+  static SmemOptIn configured;
   cudaError_t e = ensure_smem(zpass_kernel<T, LG>, smem, configured);
   if (e != cudaSuccess) return e;
   zpass_kernel<T, LG><<<blocks, threads, smem, st>>>(p);
@@ -48,7 +48,7 @@ struct StridedArgs {
 
 template <typename T, int S, int LG>
 static cudaError_t strided_lg(unsigned blocks, int threads, size_t smem, cudaStream_t st, const StridedArgs &a) {
-  static size_t configured = 48 * 1024;
+  static SmemOptIn configured;
   cudaError_t e = ensure_smem(fft_strided_kernel<T, S, LG>, smem, configured);
   if (e != cudaSuccess) return e;
   fft_strided_kernel<T, S, LG><<<blocks, threads, smem, st>>>(a.data, LG, a.lgTI, a.inner, a.tiles, a.tw, a.active,

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "pfdd_kernels.cuh"
 
@@ -102,12 +103,29 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
   return g;
 }
 
-// opts a kernel into `smem` bytes of dynamic shared memory once per size increase
+// Per-kernel record of the dynamic shared memory opted into on each device.
+// Contexts on different host threads (the server's workers) launch the same
+// kernels concurrently, so updates are serialised and only ever raise it.
+constexpr int kMaxDevices = 64;
+struct SmemOptIn {
+  std::mutex mu;
+  size_t bytes[kMaxDevices] = {};
+};
+
+// opts a kernel into `smem` bytes of dynamic shared memory on the current
+// device, once per size increase
 template <typename K>
-inline cudaError_t ensure_smem(K kernel, size_t smem, size_t &configured) {
-  if (smem <= configured) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) configured = smem;
+inline cudaError_t ensure_smem(K kernel, size_t smem, SmemOptIn &rec) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  std::lock_guard<std::mutex> lk(rec.mu);
+  if (smem <= rec.bytes[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) rec.bytes[dev] = smem;
   return e;
 }
 }  // namespace pfdd

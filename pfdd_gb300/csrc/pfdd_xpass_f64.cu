@@ -7,7 +7,7 @@ namespace pfdd {
 
 template <int NS, int LG>
 static cudaError_t launch_lg(unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p) {
-  static size_t configured = 48 * 1024;
+  static SmemOptIn configured;
   cudaError_t e = ensure_smem(x_fused_kernel<double, NS, false, LG, false>, smem, configured);
   if (e != cudaSuccess) return e;
   x_fused_kernel<double, NS, false, LG, false><<<blocks, threads, smem, st>>>(p);

@@ -30,7 +30,8 @@ EXPORTS = [
     "pfdd_required_bytes", "pfdd_fft_plan_create", "pfdd_fft_plan_destroy", "pfdd_fft_forward",
     "pfdd_fft_backward", "pfdd_status_string", "pfdd_frec", "pfdd_setfcc", "pfdd_setorient", "pfdd_seteps",
     "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
-    "pfdd_fft_device_noalloc",
+    "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
+    "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority",
 ]
 
 _lib = None
@@ -73,6 +74,7 @@ def load():
     L.pfdd_last_launch_count.restype = C.c_longlong
     L.pfdd_get_stream.argtypes = [vp]
     L.pfdd_get_stream.restype = vp
+    L.pfdd_set_stream_priority.argtypes = [vp, i]
     L.pfdd_set_kernel_timing.argtypes = [vp, i]
     L.pfdd_kernel_stat.argtypes = [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     L.pfdd_required_bytes.argtypes = [i, i, i, i, i, i]
@@ -97,6 +99,13 @@ def load():
     L.pfdd_resolve_shear.restype = None
     L.pfdd_ramp_tau.argtypes = [i, dp, i, dp]
     L.pfdd_ramp_tau.restype = None
+    ll = C.c_longlong
+    L.pfdd_server_create.argtypes = [C.POINTER(vp), i, i, sz, i, i]
+    L.pfdd_server_submit.argtypes = [vp, vp, C.POINTER(ll)]
+    L.pfdd_server_wait.argtypes = [vp, ll, dp, dp, dp]
+    L.pfdd_server_stats.argtypes = [vp, C.POINTER(ll), C.POINTER(ll), C.POINTER(ll), C.POINTER(sz)]
+    L.pfdd_server_destroy.argtypes = [vp]
+    L.pfdd_server_destroy.restype = None
     _lib = L
     return L
 

@@ -69,6 +69,15 @@ def test_argument_validation_before_any_device_call(native_lib):
         assert not h.value
     assert native_lib.pfdd_fft_plan_create(C.byref(h), 6, 8, 8, 1, 1, 0) == native.PFDD_EINVAL
     assert native_lib.pfdd_status_string(native.PFDD_ENONFINITE) == b"state became non-finite"
+    # serving form: rejected before the device is touched
+    for args in [(0, 0, 0, 0, 1), (0, 0, 0, 1, 0), (9, 0, 0, 4, 10)]:
+        assert native_lib.pfdd_server_create(C.byref(h), *args) == native.PFDD_EINVAL
+        assert not h.value
+    cnt = C.c_longlong()
+    assert native_lib.pfdd_server_submit(None, None, C.byref(cnt)) == native.PFDD_EINVAL
+    assert native_lib.pfdd_server_stats(None, None, None, None, None) == native.PFDD_EINVAL
+    assert native_lib.pfdd_server_wait(None, 1, None, None, None) == native.PFDD_EINVAL
+    native_lib.pfdd_server_destroy(None)
 
 
 def test_required_bytes_scale():
