@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg, print its JSON")
+    ap.add_argument("--batched-steps", type=int, default=100,
+                    help="timed steps of the 16-replica batched leg (0 skips it)")
+    ap.add_argument("--batched-only", action="store_true", help="run only the batched leg, print its JSON")
     ap.add_argument("--serve-scale", type=float, default=0.1,
                     help="step-count scale of the 96-request serving mix (0 skips the serving leg)")
     return ap.parse_args()
@@ -378,6 +381,51 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     }
 
 
+def run_batched(native, workloads, dev, K, K64, W=3, count=16):
+    """Batched stress sweep: `count` replicas of the 128^3 x 12 solve in one
+    context sharing B(k) (FP32-FFT form), aggregate steps/s; each replica's
+    average plastic strain against the same replicas run in the FP64 form."""
+    import torch
+    specs = workloads.config3_replicas(count)
+    xs = np.stack([workloads.initial_state(sp)[0] for sp in specs])
+    tau = np.stack([native.spec_tau(sp) for sp in specs], axis=1)   # [1000, R, ns]
+    out = {}
+    for prec, steps in (("fp32", K), ("fp64", K64)):
+        s = native.solver_for(specs[0], prec, nrep=count, device=dev)
+        s.set_state(xs)
+        stream = torch.cuda.ExternalStream(s.stream, device=f"cuda:{dev}")
+        g_w, _ = s.step(tau[:W])
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        g_t, _ = s.step(tau[W:W + steps])
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec] = {"ms": ms, "gamma": np.concatenate([g_w, g_t]), "launches": s.launches}
+        if prec == "fp32":  # per-kernel device time of a few more batched steps
+            s.kernel_timing(True)
+            s.step(tau[W + steps:W + steps + 5])
+            out[prec]["kernels"] = {nm: {"launches": c_, "avg_us": round(1e3 * t_ / c_, 1)}
+                                    for nm, (c_, t_) in s.kernel_stats().items()}
+            s.kernel_timing(False)
+        s.close()
+    kk = W + K64
+    g32, g64 = out["fp32"]["gamma"][:kk], out["fp64"]["gamma"][:kk]
+    err = np.max(np.abs(g32 - g64) / np.abs(g64), axis=0)
+    return {
+        "workload": f"{count} replicas of 128^3 x 12 (config-1 loops, noise seeds 100..{99 + count}, sigma_max "
+                    f"0.005..0.08 mu over 1000 steps), one context sharing B(k); FP32-FFT form",
+        "replicas": count, "steps": K, "warmup": W,
+        "steps_per_s": round(count * K / (out["fp32"]["ms"] / 1e3), 2),
+        "ms_per_batched_step": round(out["fp32"]["ms"] / K, 4),
+        "updates_per_s": round(count * K / (out["fp32"]["ms"] / 1e3) * 128 ** 3 * 12, 1),
+        "fp64_steps_per_s": round(count * K64 / (out["fp64"]["ms"] / 1e3), 2),
+        "strain_rel_err_vs_fp64": [float(v) for v in err], "strain_err_steps": kk,
+        "gpu_launches": int(out["fp32"]["launches"]), "kernels": out["fp32"]["kernels"],
+    }
+
+
 def run_ours(a):
     dist = Dist(a.gpus)
     import torch
@@ -387,6 +435,11 @@ def run_ours(a):
     dist.barrier()
     dev = dist.local
     torch.cuda.set_device(dev)
+    if a.batched_only:
+        print(json.dumps({"batched": run_batched(native, workloads, dev, a.batched_steps,
+                                                 max(5, a.batched_steps // 8))}), flush=True)
+        dist.close()
+        return
     if a.serve_only:
         print(json.dumps({"serving": run_serving(native, workloads, dev, a.serve_scale)}), flush=True)
         dist.close()
@@ -440,6 +493,9 @@ def run_ours(a):
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline and r64["B"] is not None:
         cpu = cpu_baseline_port(spec, r64["B"])
+    batched = None
+    if dist.world == 1 and a.batched_steps > 0:
+        batched = run_batched(native, workloads, dev, a.batched_steps, max(5, a.batched_steps // 8))
     serving = None
     if dist.world == 1 and a.serve_scale > 0:
         serving = run_serving(native, workloads, dev, a.serve_scale)
@@ -470,7 +526,7 @@ def run_ours(a):
                   "strain_rel_err_fp32_vs_fp64": strain_err, "strain_err_steps": kk},
         "kernels": kern, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(r32["launches"]), "launches_per_step": round(launches_per_step, 2),
-        "clocks": r32["clocks"], "serving": serving,
+        "clocks": r32["clocks"], "batched": batched, "serving": serving,
     }
     if dist.rank == 0:
         print(json.dumps(out), flush=True)

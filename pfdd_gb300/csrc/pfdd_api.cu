@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -204,6 +205,14 @@ struct pfdd_ctx {
   long long launches = 0;
   KTiming tm;
   std::string err;
+  // step counter on the device (the x-pass advances it, the z-pass reads it),
+  // so one captured sequence of steps replays at any position in a chunk
+  int *step_ctr = nullptr;
+  // captured CUDA graphs of kGraphSteps steps and of one step; rebuilt when a
+  // captured argument changes (gen counts those changes)
+  cudaGraphExec_t graph_many = nullptr, graph_one = nullptr;
+  unsigned gen = 0, graph_gen = ~0u;
+  bool primed = false, use_graphs = true;
 };
 
 struct pfdd_fft_plan {
@@ -325,6 +334,8 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   CK(c, cudaMalloc(&c->dslip_dev, kMaxNs * sizeof(double)));
   CK(c, cudaMalloc(&c->flag, sizeof(int)));
   CK(c, cudaMalloc(&c->errflag, sizeof(int)));
+  CK(c, cudaMalloc(&c->step_ctr, sizeof(int)));
+  if (const char *g = std::getenv("PFDD_NO_GRAPHS")) c->use_graphs = g[0] == '\0' || g[0] == '0';
   CK(c, cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st));
   CK(c, cudaMallocHost(&c->h_errflag, sizeof(int)));
   // partial sums for a chunk of steps, bounded to ~32 MB
@@ -352,8 +363,10 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->dev);
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
+  if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
-                c->active, c->flag, c->errflag, c->tw[0], c->tw[1], c->tw[2]};
+                c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2]};
   if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
   for (void *p : dp)
@@ -383,6 +396,7 @@ extern "C" pfdd_status pfdd_set_B(pfdd_ctx *c, const double *B) {
   cudaFree(tmp);
   CK(c, e);
   c->hasB = true;
+  c->gen++;  // captured x-pass arguments (B(k) constants) may differ
   return PFDD_OK;
 }
 
@@ -463,6 +477,7 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
   cudaFree(dp);
   CK(c, e);
   c->hasB = true;
+  c->gen++;  // captured x-pass arguments (B(k) constants) may differ
   return PFDD_OK;
 }
 
@@ -478,6 +493,7 @@ extern "C" pfdd_status pfdd_set_params(pfdd_ctx *c, const double *cd2, const dou
   CK(c, cudaMemcpyAsync(c->dslip_dev, c->dslip, sizeof(double) * kMaxNs, cudaMemcpyHostToDevice, c->st));
   CK(c, cudaStreamSynchronize(c->st));
   c->hasParams = true;
+  c->gen++;  // the captured z-pass arguments hold the coefficients
   return PFDD_OK;
 }
 
@@ -514,6 +530,7 @@ static pfdd_status upload_state(pfdd_ctx *c, int r0, int nr, const double *xi, c
     int any = 0;
     CK(c, cudaMemcpyAsync(&any, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(c, cudaStreamSynchronize(c->st));
+    if (c->anyBc != (any != 0)) c->gen++;  // the captured z-pass reads the mask or not
     c->anyBc = any != 0;
   }
   CK(c, cudaStreamSynchronize(c->st));
@@ -538,13 +555,17 @@ extern "C" pfdd_status pfdd_set_tau_field(pfdd_ctx *c, const double *tf) {
   if (!tf) {
     if (c->tau_field) CK(c, cudaFree(c->tau_field));
     c->tau_field = nullptr;
+    c->gen++;
     return PFDD_OK;
   }
   const size_t N = (size_t)c->N, ns = (size_t)c->ns;
   std::vector<double> t(ns * N);
   for (size_t pt = 0; pt < N; ++pt)
     for (size_t a = 0; a < ns; ++a) t[a * N + pt] = tf[pt * ns + a];
-  if (!c->tau_field) CK(c, cudaMalloc(&c->tau_field, ns * N * sizeof(double)));
+  if (!c->tau_field) {
+    CK(c, cudaMalloc(&c->tau_field, ns * N * sizeof(double)));
+    c->gen++;
+  }
   CK(c, cudaMemcpyAsync(c->tau_field, t.data(), ns * N * sizeof(double), cudaMemcpyHostToDevice, c->st));
   CK(c, cudaStreamSynchronize(c->st));
   return PFDD_OK;
@@ -592,6 +613,7 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   xp.S = c->S; xp.B = c->B; xp.active = c->active; xp.tw = c->tw[0];
   xp.inner = (long long)c->n[1] * c->n[2]; xp.tiles = c->g.xTiles;
   xp.L = c->n[0]; xp.lgL = ilog2(c->n[0]); xp.lgT = c->g.xLgT; xp.pitch = c->g.xPitch; xp.R = c->nrep;
+  xp.step_ctr = c->step_ctr;
   const unsigned blocks = (unsigned)(c->nrep * c->g.xTiles);
   t_begin(c);
   xp.bf = c->bf;
@@ -605,6 +627,33 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   return e;
 }
 
+constexpr int kGraphSteps = 16;
+
+// The launches of one TDGL step (step index taken from the device counter).
+template <typename T>
+static cudaError_t launch_step(pfdd_ctx *c, ZParams &zp) {
+  cudaError_t e = ctx_strided(c, -1, 0);
+  if (e == cudaSuccess) e = launch_x_fused<T>(c);
+  if (e == cudaSuccess) e = ctx_strided(c, +1, 0);
+  if (e == cudaSuccess) e = ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE);
+  return e;
+}
+
+// Captures `steps` steps on the context's stream into an executable graph.
+template <typename T>
+static cudaError_t capture_steps(pfdd_ctx *c, ZParams &zp, int steps, cudaGraphExec_t *out) {
+  cudaError_t e = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = cudaSuccess;
+  for (int s = 0; s < steps && le == cudaSuccess; ++s) le = launch_step<T>(c, zp);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(c->st, &g);
+  if (le != cudaSuccess) e = le;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  return e;
+}
+
 template <typename T>
 static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double *gamma, double *gamma_a) {
   ZParams zp;
@@ -612,6 +661,7 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
   zp.S = c->S; zp.xi = c->xi; zp.bc = c->anyBc ? c->bc : nullptr; zp.tau = c->tau; zp.tau_field = c->tau_field;
   zp.dslip = c->dslip_dev; zp.part = c->part; zp.err = c->errflag;
   zp.active = c->active;
+  zp.step_ctr = c->step_ctr;
   zp.tw = c->tw[2];
   zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
   zp.L = c->n[2]; zp.lgL = c->g.lgL3; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
@@ -638,12 +688,35 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
           c->h_tau[((size_t)s * c->nrep + r) * c->ns + a] = c->tau_field ? t : t / c->dslip[a];
         }
     CK(c, cudaMemcpyAsync(c->tau, c->h_tau, (size_t)ks * RF * sizeof(double), cudaMemcpyHostToDevice, c->st));
-    for (int s = 0; s < ks; ++s) {
-      CK(c, ctx_strided(c, -1, 0));
-      CK(c, launch_x_fused<T>(c));
-      CK(c, ctx_strided(c, +1, 0));
-      zp.step = s;
-      CK(c, ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE));
+    CK(c, cudaMemsetAsync(c->step_ctr, 0xff, sizeof(int), c->st));  // -1: the first x-pass makes it 0
+    int done = 0;
+    const bool direct = c->tm.on || !c->use_graphs;
+    if (direct || !c->primed) {
+      // direct launches: timing mode, and the first step of a context (it
+      // also sets every kernel's shared-memory opt-in before any capture)
+      const int n = direct ? ks : 1;
+      for (; done < n; ++done) CK(c, launch_step<T>(c, zp));
+      c->primed = true;
+    }
+    if (done < ks) {
+      if (c->graph_gen != c->gen) {
+        if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
+        if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
+        c->graph_many = c->graph_one = nullptr;
+        const long long l0 = c->launches;
+        CK(c, capture_steps<T>(c, zp, kGraphSteps, &c->graph_many));
+        CK(c, capture_steps<T>(c, zp, 1, &c->graph_one));
+        c->launches = l0;  // captured, not launched
+        c->graph_gen = c->gen;
+      }
+      for (; done + kGraphSteps <= ks; done += kGraphSteps) {
+        CK(c, cudaGraphLaunch(c->graph_many, c->st));
+        c->launches += 4LL * kGraphSteps;
+      }
+      for (; done < ks; ++done) {
+        CK(c, cudaGraphLaunch(c->graph_one, c->st));
+        c->launches += 4;
+      }
     }
     const int nt = ks * c->nrep;
     t_begin(c);

@@ -41,6 +41,7 @@ struct ZParams {
   const uint8_t *active;    // [R] or null
   const void *tw;           // forward twiddles of length L
   int *err;                 // set when a bounded wait times out (may be null)
+  const int *step_ctr;      // step index within the chunk, advanced by the x-pass (null: use `step`)
   long long N, lines_per_field;
   int step, L, lgL, ns, R, TL, nparts, flags, pitch;
   double inv_n, uq2;
@@ -179,7 +180,8 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
     mbar_wait(&xbar, 0, p.err);
     __syncthreads();  // the update reads elements of other teams' lines
     const UpdCoef<T> k(p, a);
-    const double tv = p.tau[((long long)p.step * p.R + r) * p.ns + a];
+    const int step = p.step_ctr ? *p.step_ctr : p.step;
+    const double tv = p.tau[((long long)step * p.R + r) * p.ns + a];
     const auto ctau0 = k.tau(tv);
     const long long fbase = rf * p.N;  // bit / element base of this field
     long long acc = 0;
@@ -242,7 +244,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
     const long long s = block_sum_i64(acc, red);
     const int anybig = __syncthreads_or(big);
     if (tid == 0)
-      p.part[((long long)p.step * p.R * p.ns + rf) * p.nparts + lf0 / TL] =
+      p.part[((long long)step * p.R * p.ns + rf) * p.nparts + lf0 / TL] =
           anybig ? __longlong_as_double(0x7ff8000000000000ll) : (double)s * 0x1p-44;
     __syncthreads();
   }
@@ -320,6 +322,7 @@ struct XParams {
   long long inner, tiles;  // inner = N2*N3, tiles = inner / T per field row
   int L, lgL, lgT, pitch, R;
   int *err;                // set when a bounded wait times out (may be null)
+  int *step_ctr;           // incremented once per launch (null: none); the z-pass reads it
   BFlyParams bf;
 };
 
@@ -362,6 +365,7 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   T *Bs = reinterpret_cast<T *>(smraw + head);
   const long long r = blockIdx.x / p.tiles;
   const long long tile = blockIdx.x - r * p.tiles;
+  if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
   if (p.active && !p.active[r]) return;
   const long long c0 = tile << lgT;
   const int npt = L << lgT;
