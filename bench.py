@@ -211,8 +211,9 @@ def time_form(native, workloads, spec, prec, W, K, device, dist, clocks=None, pr
         kstats = s.kernel_stats()
         s.kernel_timing(False)
     B = s.get_B() if prec == "fp64" else None
+    plan = s.plan()
     s.close()
-    return dict(ms=ms, launches=launches, gamma=g[:, 0], gamma_a=ga[:, 0], clocks=clk, kstats=kstats, B=B)
+    return dict(ms=ms, launches=launches, gamma=g[:, 0], gamma_a=ga[:, 0], clocks=clk, kstats=kstats, B=B, plan=plan)
 
 
 def time_e2e(native, workloads, spec, prec, K, device):
@@ -402,7 +403,7 @@ def run_batched(native, workloads, dev, K, K64, W=3, count=16):
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        out[prec] = {"ms": ms, "gamma": np.concatenate([g_w, g_t]), "launches": s.launches}
+        out[prec] = {"ms": ms, "gamma": np.concatenate([g_w, g_t]), "launches": s.launches, "plan": s.plan()}
         if prec == "fp32":  # per-kernel device time of a few more batched steps
             s.kernel_timing(True)
             s.step(tau[W + steps:W + steps + 5])
@@ -423,6 +424,7 @@ def run_batched(native, workloads, dev, K, K64, W=3, count=16):
         "fp64_steps_per_s": round(count * K64 / (out["fp64"]["ms"] / 1e3), 2),
         "strain_rel_err_vs_fp64": [float(v) for v in err], "strain_err_steps": kk,
         "gpu_launches": int(out["fp32"]["launches"]), "kernels": out["fp32"]["kernels"],
+        "plan": out["fp32"]["plan"],
     }
 
 
@@ -524,7 +526,7 @@ def run_ours(a):
                                         "(no stored table)"},
                   "ratio_fp32_over_fp64": round(v32 / v64, 2),
                   "strain_rel_err_fp32_vs_fp64": strain_err, "strain_err_steps": kk},
-        "kernels": kern, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "kernels": kern, "plan": r32["plan"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(r32["launches"]), "launches_per_step": round(launches_per_step, 2),
         "clocks": r32["clocks"], "batched": batched, "serving": serving,
     }

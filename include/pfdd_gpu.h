@@ -147,6 +147,13 @@ pfdd_status pfdd_set_stream_priority(pfdd_ctx *ctx, int priority);
 pfdd_status pfdd_set_kernel_timing(pfdd_ctx *ctx, int enable);
 pfdd_status pfdd_kernel_stat(pfdd_ctx *ctx, int idx, const char **name, long long *launches, double *total_ms);
 
+/* Launch plan of the context as a JSON object: tile widths, threads and shared
+ * memory of each pass, the radix plan of each axis, the steps per captured CUDA
+ * graph and the autotune timings (null before the first pfdd_step, which times
+ * every x-pass and y-pass tile width that fits and keeps the fastest; set
+ * PFDD_NO_TUNE=1 to keep the defaults).  No counterpart in the reference. */
+pfdd_status pfdd_get_plan(pfdd_ctx *ctx, char *buf, size_t len);
+
 /* Device bytes held by a context of this shape (admission control). */
 size_t pfdd_required_bytes(int n1, int n2, int n3, int ns, int nrep, int precision);
 

@@ -213,6 +213,9 @@ struct pfdd_ctx {
   cudaGraphExec_t graph_many = nullptr, graph_one = nullptr;
   unsigned gen = 0, graph_gen = ~0u;
   bool primed = false, use_graphs = true;
+  // launch plan: tile widths timed on the first step (autotune), as JSON
+  bool tuned = false, tune = true;
+  std::string plan;
 };
 
 struct pfdd_fft_plan {
@@ -264,6 +267,20 @@ static void t_end(pfdd_ctx *c, int id) {
   c->tm.used += 2;
 }
 
+// Stockham radices of a line of length n (radix 8 while at least 8 remain).
+static std::string radix_plan(int n) {
+  std::string r;
+  int lg = 0;
+  while ((1 << lg) < n) ++lg;
+  if (lg == 0) return "1";
+  while (lg > 0) {
+    const int k = lg >= 3 ? 3 : lg;
+    r += (r.empty() ? "" : "x") + std::to_string(1 << k);
+    lg -= k;
+  }
+  return r;
+}
+
 static size_t vsize_of(int prec) { return prec == PFDD_FP64 ? sizeof(double2) : sizeof(float2); }
 // bytes of a stored B(k) value; 0: the x-pass evaluates B(k) itself
 static size_t bsize_of(int prec) {
@@ -310,6 +327,9 @@ static cudaError_t make_twiddles(void **tw, const int n[3], int prec, cudaStream
   return cudaSuccess;
 }
 
+template <typename T>
+static pfdd_status autotune(pfdd_ctx *c);
+
 extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n3, int ns, int nrep, int precision,
                                            int device) {
   if (!out) return PFDD_EINVAL;
@@ -325,7 +345,6 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   CK(c, cudaSetDevice(device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision));
-  c->bl = BLayout{c->N, (long long)n2 * n3, n1, c->g.xLgT, ns * (ns + 1) / 2};
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
   CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
   CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
@@ -336,6 +355,7 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   CK(c, cudaMalloc(&c->errflag, sizeof(int)));
   CK(c, cudaMalloc(&c->step_ctr, sizeof(int)));
   if (const char *g = std::getenv("PFDD_NO_GRAPHS")) c->use_graphs = g[0] == '\0' || g[0] == '0';
+  if (const char *g = std::getenv("PFDD_NO_TUNE")) c->tune = g[0] == '\0' || g[0] == '0';
   CK(c, cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st));
   CK(c, cudaMallocHost(&c->h_errflag, sizeof(int)));
   // partial sums for a chunk of steps, bounded to ~32 MB
@@ -351,6 +371,15 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   CK(c, make_twiddles(c->tw, c->n, precision, c->st));
   c->h_active.assign(nrep, 1);
   CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), nrep, cudaMemcpyHostToDevice, c->st));
+  // tile widths are timed on the (zeroed) buffers before B(k) is laid out in
+  // the chosen x-pass tile order
+  CK(c, cudaMemsetAsync(c->S, 0, RF * N * vsize_of(precision), c->st));
+  if (c->B) CK(c, cudaMemsetAsync(c->B, 0, P * N * bsize_of(precision), c->st));
+  {
+    const pfdd_status st = precision == PFDD_FP64 ? autotune<double>(c) : autotune<float>(c);
+    if (st != PFDD_OK) return st;
+  }
+  c->bl = BLayout{c->N, (long long)n2 * n3, n1, c->g.xLgT, ns * (ns + 1) / 2};
   CK(c, cudaStreamSynchronize(c->st));
   return PFDD_OK;
 }
@@ -629,6 +658,88 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
 
 constexpr int kGraphSteps = 16;
 
+static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
+  const Geometry &g = c->g;
+  char b[768];
+  snprintf(b, sizeof b,
+           "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld}, "
+           "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas_per_field_plane\": %lld}, "
+           "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
+           "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": %s}",
+           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, 1 << g.lgTI[0], g.threads[0], g.smem[0],
+           g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0]).c_str(), radix_plan(c->n[1]).c_str(),
+           radix_plan(c->n[2]).c_str(), kGraphSteps, tuning.c_str());
+  return b;
+}
+
+// Times every tile width of the fused x-pass and of the y-pass that fits, on
+// the context's own buffers (3 launches each after one warm-up), and keeps the
+// fastest.  Tile widths change no result: every line and every point is
+// computed by the same instructions whatever the tile.  The trial launches
+// overwrite the spectral buffer, which the next step rebuilds from xi.
+template <typename T>
+static pfdd_status autotune(pfdd_ctx *c) {
+  c->tuned = true;
+  std::string tuning = "null";
+  if (c->tune) {
+    const bool timing = c->tm.on;
+    c->tm.on = false;
+    const long long l0 = c->launches;
+    cudaEvent_t e0, e1;
+    CK(c, cudaEventCreate(&e0));
+    CK(c, cudaEventCreate(&e1));
+    auto time_us = [&](auto launch) -> double {
+      if (launch() != cudaSuccess) { cudaGetLastError(); return -1.0; }
+      cudaEventRecord(e0, c->st);
+      for (int i = 0; i < 3; ++i)
+        if (launch() != cudaSuccess) { cudaGetLastError(); return -1.0; }
+      cudaEventRecord(e1, c->st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return -1.0;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      return 1e3 * ms / 3.0;
+    };
+    std::string xs, ys;
+    const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
+    Geometry best = c->g;
+    double bt = 1e30;
+    for (int lgT = 0; lgT <= 6; ++lgT) {
+      Geometry g = c->g;
+      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT)) continue;
+      c->g = g;
+      const double us = time_us([&] { return launch_x_fused<T>(c); });
+      if (us > 0 && us < bt) { bt = us; best = g; }
+      char b[64];
+      snprintf(b, sizeof b, "%s\"%d\": %.1f", xs.empty() ? "" : ", ", 1 << lgT, us);
+      xs += b;
+    }
+    c->g = best;
+    if (c->n[1] > 1) {
+      bt = 1e30;
+      for (int lgTI = 0; lgTI <= 7; ++lgTI) {
+        Geometry g = c->g;
+        if (!set_strided_geometry(g, 0, c->n[1], c->n[2], lgTI, vs)) continue;
+        c->g = g;
+        const double us = time_us([&] { return ctx_strided(c, -1, 0); });
+        if (us > 0 && us < bt) { bt = us; best = g; }
+        char b[64];
+        snprintf(b, sizeof b, "%s\"%d\": %.1f", ys.empty() ? "" : ", ", 1 << lgTI, us);
+        ys += b;
+      }
+      c->g = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->launches = l0;
+    c->tm.on = timing;
+    c->specValid = false;
+    c->gen++;  // captured launch shapes change
+    tuning = "{\"x_pass_us_by_tile\": {" + xs + "}, \"y_pass_us_by_tile\": {" + ys + "}}";
+  }
+  c->plan = plan_json(c, tuning);
+  return PFDD_OK;
+}
+
 // The launches of one TDGL step (step index taken from the device counter).
 template <typename T>
 static cudaError_t launch_step(pfdd_ctx *c, ZParams &zp) {
@@ -755,6 +866,14 @@ extern "C" pfdd_status pfdd_step(pfdd_ctx *c, int nsteps, const double *tau, dou
   CK(c, cudaSetDevice(c->dev));
   return c->prec == PFDD_FP64 ? run_steps<double>(c, nsteps, tau, gamma, gamma_a)
                               : run_steps<float>(c, nsteps, tau, gamma, gamma_a);
+}
+
+extern "C" pfdd_status pfdd_get_plan(pfdd_ctx *c, char *buf, size_t len) {
+  if (!c || !buf || len == 0) return fail(c, PFDD_EINVAL, "pfdd_get_plan: bad argument");
+  const std::string p = c->tuned ? c->plan : plan_json(c, "null");
+  if (p.size() + 1 > len) return fail(c, PFDD_EINVAL, "pfdd_get_plan: buffer of %zu bytes, need %zu", len, p.size() + 1);
+  std::memcpy(buf, p.c_str(), p.size() + 1);
+  return PFDD_OK;
 }
 
 extern "C" pfdd_status pfdd_get_state(pfdd_ctx *c, double *xi) {

@@ -152,6 +152,43 @@ __device__ __forceinline__ void line_fft(int th, int lgL_rt, const V *tw, Addr s
   }
 }
 
+// Same transform (compile-time L = 2^LG >= 8) with register input and/or a
+// direct output.  IN_REGS: v[m] already holds line[th + m*L/8] (loaded by the
+// caller straight from global memory), so the first stage skips its shared-
+// memory read.  OUT_DIRECT: the last stage writes through `out` (e.g. global
+// memory, natural order) instead of `sm`, and no barrier follows it.  `sm`
+// holds the line between stages; every thread of the block must call it.
+template <int S, int LG, bool IN_REGS, bool OUT_DIRECT, typename V, typename AddrS, typename AddrO>
+__device__ __forceinline__ void line_fft_io(V *v, int th, const V *tw, AddrS sm, AddrO out, bool active) {
+  static_assert(LG >= 3, "line_fft_io needs L >= 8");
+  constexpr int NST = (LG + 2) / 3;
+  constexpr int L8 = 1 << (LG - 3);
+#pragma unroll
+  for (int st = 0; st < NST; ++st) {
+    const int lgNs = 3 * st;
+    const int rem = LG - lgNs;
+    if (st > 0 || !IN_REGS) {
+      if (active) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) v[m] = *sm(th + m * L8);
+      }
+      __syncthreads();  // every read of this stage precedes its in-place writes
+    }
+    if (active) {
+      if (OUT_DIRECT && st == NST - 1) {
+        if (rem >= 3) stockham_stage<S, 8>(v, th, LG, lgNs, tw, out);
+        else if (rem == 2) stockham_stage<S, 4>(v, th, LG, lgNs, tw, out);
+        else stockham_stage<S, 2>(v, th, LG, lgNs, tw, out);
+      } else {
+        if (rem >= 3) stockham_stage<S, 8>(v, th, LG, lgNs, tw, sm);
+        else if (rem == 2) stockham_stage<S, 4>(v, th, LG, lgNs, tw, sm);
+        else stockham_stage<S, 2>(v, th, LG, lgNs, tw, sm);
+      }
+    }
+    if (!(OUT_DIRECT && st == NST - 1)) __syncthreads();
+  }
+}
+
 // Copies a length-L twiddle table to shared memory (caller synchronises).
 template <typename V>
 __device__ __forceinline__ void load_twiddles(V *dst, const V *__restrict__ src, int L) {

@@ -274,6 +274,21 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
   V *base = reinterpret_cast<V *>(data_) + o * (long long)L * inner + c0;
   const int nel = L << lgTI, tid = threadIdx.x, nthr = blockDim.x;
   load_twiddles(tws, reinterpret_cast<const V *>(tw_), L);
+  if constexpr (LG >= 3) {
+    // lines straight from global memory into registers (consecutive lanes on
+    // consecutive columns: coalesced), the last stage straight back; shared
+    // memory only between stages.  The first stage uses no twiddles, and the
+    // barrier after it orders the twiddle table before the second.
+    constexpr int L8 = 1 << (LG - 3);
+    const int t = tid & (TI - 1), th = tid >> lgTI;
+    V *col = base + t;
+    V v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = col[(long long)(th + m * L8) * inner];
+    line_fft_io<S, LG, true, true>(v, th, tws, [&](int l) { return &sm[l * pitch + t]; },
+                                   [&](int l) { return &col[(long long)l * inner]; }, true);
+    return;
+  }
   for (int e = tid; e < nel; e += nthr) {
     const int l = e >> lgTI, t = e & (TI - 1);
     cp_async_elem(&sm[l * pitch + t], &base[(long long)l * inner + t]);
@@ -346,8 +361,10 @@ __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, 
 // all NS fields of one replica: forward FFT along x, k-space contraction
 // S[a](k) <- sum_b B_ab(k) S[b](k) (F:4609-4629, b ascending), inverse FFT
 // along x.  Shared memory: twiddles [L] | tile [a][t][x] (x contiguous, odd
-// line pitch) | B tile [P][T*L].  The S tile and the B tile arrive by cp.async in
-// two groups, so the B fetch overlaps the forward FFT.  One point per thread
+// line pitch) | B tile [P][T*L].  With a compile-time line length the lines
+// come from global memory straight into registers and the inverse FFT's last
+// stage writes them straight back (shared memory only between stages); the B
+// tile streams in by TMA bulk copies during the forward FFT.  One point per thread
 // in the contraction; IN_REGS keeps its NS inputs in registers (FP32, up to
 // 384 threads); FP64 reads them from shared memory and runs at most 256 threads.
 // BFLY (FP32 only): B_ab(k) = (E_ab - u_a . t_b) / mu with t_b = sigma_b f and
@@ -374,13 +391,20 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nel = (NS * L) << lgT;
   auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + x; };
-  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
-  // S tile: e -> (a, x, t) with t fastest (contiguous in memory)
-  for (int e = tid; e < nel; e += nthr) {
-    const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
-    cp_async_elem(&sm[sidx(a, t, x)], &S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t]);
+  // line (a, t) of the tile in global memory: element x at gline(a, t)[x * inner]
+  auto gline = [&](int a, int t) { return S + ((long long)r * NS + a) * L * p.inner + c0 + t; };
+  const int E = L >= 8 ? 8 : L, team = L / E, teams = nthr / team;
+  const int lines = NS << lgT;
+  const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
+  constexpr bool kDirect = LG >= 3;  // compile-time line length: lines go global <-> registers
+  if constexpr (!kDirect) {
+    // S tile: e -> (a, x, t) with t fastest (contiguous in memory)
+    for (int e = tid; e < nel; e += nthr) {
+      const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
+      cp_async_elem(&sm[sidx(a, t, x)], &S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t]);
+    }
+    cp_async_commit();
   }
-  cp_async_commit();
   // B tile: one contiguous block of P * npt values, TMA bulk copies issued by
   // one thread so it streams in during the forward FFT
   __shared__ __align__(8) uint64_t bbar;
@@ -392,14 +416,28 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   }
   if (!BFLY && !bulk)
     for (int i = tid; i < P * npt; i += nthr) Bs[i] = Bt[i];
-  cp_async_wait<0>();
-  __syncthreads();
-  const int E = L >= 8 ? 8 : L, team = L / E, teams = nthr / team;
-  const int lines = NS << lgT;
-  const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
-  for (int l0 = 0; l0 < lines; l0 += teams) {
-    const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-    line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  if constexpr (kDirect) {
+    constexpr int L8 = 1 << (LG - 3);
+    for (int l0 = 0; l0 < lines; l0 += teams) {
+      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+      const bool act = ln < lines;
+      V v[8];
+      if (act) {
+        const V *g = gline(a, t);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) v[m] = g[(long long)(th + m * L8) * p.inner];
+      }
+      auto line = [&](int l) { return &sm[sidx(a, t, l)]; };
+      line_fft_io<-1, LG, true, false>(v, th, tws, line, line, act);
+    }
+  } else {
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int l0 = 0; l0 < lines; l0 += teams) {
+      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+      line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+    }
   }
   if (bulk) mbar_wait(&bbar, 0, p.err);
   __syncthreads();
@@ -474,14 +512,24 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
     for (int a = 0; a < NS; ++a) sm[sidx(a, t, x)] = out[a];
   }
   __syncthreads();
-  for (int l0 = 0; l0 < lines; l0 += teams) {
-    const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-    line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
-  }
-  __syncthreads();
-  for (int e = tid; e < nel; e += nthr) {
-    const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
-    S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t] = sm[sidx(a, t, x)];
+  if constexpr (kDirect) {
+    for (int l0 = 0; l0 < lines; l0 += teams) {
+      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+      V v[8];
+      V *g = gline(a, t);
+      line_fft_io<+1, LG, false, true>(v, th, tws, [&](int l) { return &sm[sidx(a, t, l)]; },
+                                       [&](int l) { return &g[(long long)l * p.inner]; }, ln < lines);
+    }
+  } else {
+    for (int l0 = 0; l0 < lines; l0 += teams) {
+      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+      line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+    }
+    __syncthreads();
+    for (int e = tid; e < nel; e += nthr) {
+      const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
+      S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t] = sm[sidx(a, t, x)];
+    }
   }
 }
 

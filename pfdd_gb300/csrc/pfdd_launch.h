@@ -54,8 +54,45 @@ struct Geometry {
 
 inline int line_pitch(int L) { return L + 1; }  // odd pitch: lanes on different lines hit different banks
 
+// Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.
+inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, int lgTI, size_t vsize) {
+  const int E = std::min(8, L), team = L / E;
+  const int TI = 1 << lgTI;
+  if (TI > inner || (long long)TI * team > kThreads) return false;  // fft_strided_kernel launch bounds
+  g.lgTI[ax] = lgTI;
+  g.threads[ax] = TI * team;
+  g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
+  g.tiles[ax] = inner / TI;
+  g.smem[ax] = ((size_t)L + (size_t)L * g.pitch[ax]) * vsize;
+  return g.smem[ax] <= 200 * 1024;
+}
+
+// Fused x-pass with tiles of T = 2^lgT inner indices (all N1 x, all ns fields,
+// the tile's B(k)).  False when the tile does not fit.
+inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT) {
+  const long long innerx = (long long)n2 * n3;
+  if ((1LL << lgT) > innerx) return false;
+  const int pitch = line_pitch(n1);
+  const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize);
+  if (smem > 200 * 1024) return false;
+  const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
+  const int unit = std::max(32, team);
+  const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
+  if (unit > cap) return false;
+  int thr = std::min(cap, std::max(npt, lines * team));
+  thr = (thr + unit - 1) / unit * unit;
+  g.xPitch = pitch;
+  g.xLgT = lgT;
+  g.xTiles = innerx >> lgT;
+  g.xSmem = smem;
+  g.xThreads = std::min(thr, cap / unit * unit);
+  return true;
+}
+
 // ns = 0: no fused x-pass (FFT-boundary plans).  bsize: bytes of a stored B(k)
-// value, 0 when the x-pass evaluates B(k) itself.
+// value, 0 when the x-pass evaluates B(k) itself.  The strided and x-pass tile
+// widths chosen here are the defaults; a context's first step may retune them
+// (they do not change any result).
 inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize) {
   Geometry g;
   const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
@@ -75,30 +112,15 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
     const int L = Ls[ax], E = std::min(8, L), team = L / E;
     int TI = std::max(1, kThreads / team);
     while ((long long)TI > inner[ax]) TI >>= 1;
-    g.lgTI[ax] = ilog2(TI);
-    g.threads[ax] = TI * team;
-    g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
-    g.tiles[ax] = inner[ax] / TI;
-    g.smem[ax] = ((size_t)L + (size_t)L * g.pitch[ax]) * vsize;
+    set_strided_geometry(g, ax, L, inner[ax], ilog2(TI), vsize);
   }
   if (ns > 0) {
-    // x-pass tile: T consecutive inner indices of all N1 x and all ns fields plus
-    // the tile's B(k), sized for two CTAs per SM (<= 110 KB), T <= 32
-    const long long innerx = (long long)n2 * n3;
-    g.xPitch = line_pitch(n1);
+    // default x tile: the widest T <= 32 whose tile fits two CTAs per SM (<= 110 KB)
     int lgT = 5;
-    while (lgT > 0 && ((1LL << lgT) > innerx ||
-                       x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize) > 110 * 1024))
+    while (lgT > 0 && ((1LL << lgT) > (long long)n2 * n3 ||
+                       x_fused_smem(ns, n1, lgT, line_pitch(n1), vsize, bsize) > 110 * 1024))
       --lgT;
-    g.xLgT = lgT;
-    g.xTiles = innerx >> lgT;
-    g.xSmem = x_fused_smem(ns, n1, lgT, g.xPitch, vsize, bsize);
-    const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
-    const int unit = std::max(32, team);
-    const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
-    int thr = std::min(cap, std::max(npt, lines * team));
-    thr = (thr + unit - 1) / unit * unit;
-    g.xThreads = std::min(thr, cap / unit * unit);
+    set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
   }
   return g;
 }

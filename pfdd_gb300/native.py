@@ -31,7 +31,7 @@ EXPORTS = [
     "pfdd_fft_backward", "pfdd_status_string", "pfdd_frec", "pfdd_setfcc", "pfdd_setorient", "pfdd_seteps",
     "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
     "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
-    "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority",
+    "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority", "pfdd_get_plan",
 ]
 
 _lib = None
@@ -75,6 +75,7 @@ def load():
     L.pfdd_get_stream.argtypes = [vp]
     L.pfdd_get_stream.restype = vp
     L.pfdd_set_stream_priority.argtypes = [vp, i]
+    L.pfdd_get_plan.argtypes = [vp, C.c_char_p, sz]
     L.pfdd_set_kernel_timing.argtypes = [vp, i]
     L.pfdd_kernel_stat.argtypes = [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     L.pfdd_required_bytes.argtypes = [i, i, i, i, i, i]
@@ -259,6 +260,13 @@ class Solver:
 
     def kernel_timing(self, on: bool):
         self._check(self.L.pfdd_set_kernel_timing(self.h, int(bool(on))), "pfdd_set_kernel_timing")
+
+    def plan(self) -> dict:
+        """Launch plan (tile widths, threads, shared memory, radix plans, autotune timings)."""
+        import json
+        buf = C.create_string_buffer(4096)
+        self._check(self.L.pfdd_get_plan(self.h, buf, len(buf)), "pfdd_get_plan")
+        return json.loads(buf.value.decode())
 
     def kernel_stats(self) -> dict:
         """{kernel name: (timed launches, total device ms)} since timing was enabled."""

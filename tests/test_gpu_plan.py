@@ -1,0 +1,44 @@
+"""Launch plan and autotuning: the plan is reported, every tile width tried by the
+autotuner is one that fits, and the tuned context gives the same bits as the
+default plan (tile widths do not change any result)."""
+import os
+
+import numpy as np
+import pytest
+
+from pfdd_gb300 import native, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def run(spec, precision, tune):
+    old = os.environ.get("PFDD_NO_TUNE")
+    os.environ["PFDD_NO_TUNE"] = "0" if tune else "1"
+    try:
+        s = native.solver_for(spec, precision)
+    finally:
+        if old is None:
+            del os.environ["PFDD_NO_TUNE"]
+        else:
+            os.environ["PFDD_NO_TUNE"] = old
+    x0, b0 = workloads.initial_state(spec)
+    s.set_state(x0, b0)
+    g, ga = s.step(native.spec_tau(spec))
+    out = (g, s.get_state(), s.plan())
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp32_bfly"])
+def test_tuned_plan_gives_same_bits(native_lib, precision):
+    spec = workloads.SolveSpec(n=(32, 16, 64), ns=12, steps=12, sigma_max=0.05, noise_seed=21,
+                               loops=workloads.random_loops((32, 16, 64), 4, 2.0, 6.0, 12, seed=21))
+    g1, x1, p1 = run(spec, precision, True)
+    g0, x0, p0 = run(spec, precision, False)
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(x1, x0)
+    assert p0["autotune"] is None
+    tried = p1["autotune"]["x_pass_us_by_tile"]
+    assert len(tried) >= 1 and all(v > 0 for v in tried.values())
+    assert str(p1["x_pass"]["tile_columns"]) in tried
+    assert p1["radix_plan"] == ["8x4", "8x2", "8x8"]
