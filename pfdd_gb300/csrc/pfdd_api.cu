@@ -344,7 +344,7 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   c->N = (long long)n1 * n2 * n3;
   CK(c, cudaSetDevice(device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-  c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision));
+  c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision), /*xfast=*/true);
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
   CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
   CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
@@ -624,8 +624,11 @@ static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/) {
   const int L = ax == 0 ? c->n[1] : c->n[0];
   if (L == 1) return cudaSuccess;
   const int gi = ax == 0 ? 0 : 1;
-  const long long inner = ax == 0 ? (long long)c->n[2] : (long long)c->n[1] * c->n[2];
-  const long long outer = ax == 0 ? (long long)c->nrep * c->ns * c->n[0] : (long long)c->nrep * c->ns;
+  // y lines: stride N3*N1 in the x-fastest layout, N3 in the natural one
+  const long long inner = ax == 0 ? (c->g.xfast ? (long long)c->n[2] * c->n[0] : (long long)c->n[2])
+                                  : (long long)c->n[1] * c->n[2];
+  const long long outer = ax == 0 ? (long long)c->nrep * c->ns * (c->g.xfast ? 1 : c->n[0])
+                                  : (long long)c->nrep * c->ns;
   const long long outer_per_rep = outer / c->nrep;
   const long long blocks = outer * c->g.tiles[gi];
   t_begin(c);
@@ -663,7 +666,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   char b[768];
   snprintf(b, sizeof b,
            "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld}, "
-           "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas_per_field_plane\": %lld}, "
+           "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
            "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
            "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": %s}",
            1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, 1 << g.lgTI[0], g.threads[0], g.smem[0],
@@ -718,7 +721,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
       bt = 1e30;
       for (int lgTI = 0; lgTI <= 7; ++lgTI) {
         Geometry g = c->g;
-        if (!set_strided_geometry(g, 0, c->n[1], c->n[2], lgTI, vs)) continue;
+        if (!set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], lgTI, vs)) continue;
         c->g = g;
         const double us = time_us([&] { return ctx_strided(c, -1, 0); });
         if (us > 0 && us < bt) { bt = us; best = g; }
@@ -777,6 +780,8 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
   zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
   zp.L = c->n[2]; zp.lgL = c->g.lgL3; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
   zp.pitch = c->g.zPitch;
+  zp.sxf = c->g.xfast ? 1 : 0;
+  zp.n1 = c->n[0]; zp.n2 = c->n[1]; zp.lgTL = ilog2(c->g.zTL);
   zp.inv_n = 1.0 / (double)c->N;  // N is a power of two: exact, same as dividing by nsize
   zp.uq2 = c->uq2;
   for (int a = 0; a < c->ns; ++a) {

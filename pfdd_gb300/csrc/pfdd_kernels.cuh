@@ -44,6 +44,10 @@ struct ZParams {
   const int *step_ctr;      // step index within the chunk, advanced by the x-pass (null: use `step`)
   long long N, lines_per_field;
   int step, L, lgL, ns, R, TL, nparts, flags, pitch;
+  // S layout: 0 = natural [x][y][z] (z fastest, like xi); 1 = x fastest,
+  // [y][z][x] per field (the step's spectral buffer).  With 1 a block takes the
+  // TL lines (x0..x0+TL-1, y) and n1, n2, lgTL describe the grid.
+  int sxf, n1, n2, lgTL;
   double inv_n, uq2;
   double cd2[kMaxNs], asf_pi[kMaxNs], uq2cd2[kMaxNs];
 };
@@ -131,10 +135,12 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *red) 
   return s;
 }
 
-// z-pass: TL contiguous lines of length L (one field), see ZFlags.
+// z-pass: TL lines of length L along z (one field), see ZFlags.
 // Shared memory: twiddles [L] | S lines [TL][pitch] (odd pitch) | xi tile
-// [TL*L] double2 (update only).  The S lines and the xi tile are fetched with
-// cp.async in two completion groups so the xi fetch overlaps the inverse FFT.
+// [TL][L] double2 (update only).  The S lines arrive by cp.async, the FP64 xi
+// lines by TMA bulk copies that overlap the inverse FFT.  Natural layout: the
+// block's lines are consecutive (x, y) pairs; x-fastest S layout (sxf): the
+// lines (x0 + t, y) of one y, whose S values sit TL to a contiguous run.
 template <typename T, int LG>
 __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   using V = typename cpx<T>::t;
@@ -150,23 +156,45 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   const int r = (int)(rf / p.ns), a = (int)(rf % p.ns);
   if (p.active && !p.active[r]) return;
   const long long lf0 = line0 - rf * p.lines_per_field;
-  const long long e0 = line0 << lgL;
+  const bool xf = p.sxf != 0;
+  // block within the field -> (x block, y) for the x-fastest layout (x block fastest)
+  const int xblocks = xf ? p.n1 >> p.lgTL : 1;
+  const int bf = (int)(lf0 / TL);
+  const int x0 = xf ? (bf % xblocks) * TL : 0, yj = xf ? bf / xblocks : 0;
+  // element offset of line t within the field (xi layout, natural)
+  auto lineoff = [&](int t) -> long long { return xf ? ((long long)(x0 + t) * p.n2 + yj) * L : (lf0 + t) * L; };
+  const long long fbase = rf * p.N;  // element / bit base of this field
   const int nel = TL << lgL;
   const int tid = threadIdx.x, nthr = blockDim.x;
   V *S = reinterpret_cast<V *>(p.S);
   const bool upd = (p.flags & Z_UPDATE) != 0;
   auto sidx = [&](int e) { return (e >> lgL) * P + (e & (L - 1)); };
+  // S element (line t, z = k) in global memory
+  auto sg = [&](int t, int k) -> V * {
+    return xf ? &S[fbase + ((long long)yj * L + k) * p.n1 + x0 + t] : &S[fbase + (lf0 + t) * L + k];
+  };
 
   __shared__ __align__(8) uint64_t xbar;  // completion of the FP64 state tile
-  if (upd && tid == 0) {  // the state tile is one contiguous block: TMA bulk copies
+  if (upd && tid == 0) {  // TMA bulk copies: one block (natural) or one per line
     mbar_init(&xbar, 1);
-    bulk_load(xs, p.xi + e0, (unsigned)nel * 16u, &xbar);
+    mbar_arrive_expect_tx(&xbar, (unsigned)nel * 16u);
+    if (xf)
+      for (int t = 0; t < TL; ++t) bulk_copy(xs + (t << lgL), p.xi + fbase + lineoff(t), (unsigned)L * 16u, &xbar);
+    else
+      bulk_copy(xs, p.xi + fbase + lf0 * L, (unsigned)nel * 16u, &xbar);
   }
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   if (p.flags & Z_SRC_XI) {
-    for (int e = tid; e < nel; e += nthr) sm[sidx(e)] = from_xi<V>(p.xi[e0 + e]);
+    for (int e = tid; e < nel; e += nthr)
+      sm[sidx(e)] = from_xi<V>(p.xi[fbase + lineoff(e >> lgL) + (e & (L - 1))]);
+  } else if (xf) {
+    // consecutive lanes on consecutive x: TL-element runs in global memory
+    for (int e = tid; e < nel; e += nthr) {
+      const int t = e & (TL - 1), k = e >> p.lgTL;
+      cp_async_elem(&sm[t * P + k], sg(t, k));
+    }
   } else {
-    for (int e = tid; e < nel; e += nthr) cp_async_elem(&sm[sidx(e)], &S[e0 + e]);
+    for (int e = tid; e < nel; e += nthr) cp_async_elem(&sm[sidx(e)], sg(e >> lgL, e & (L - 1)));
   }
   cp_async_commit();
   cp_async_wait<0>();
@@ -183,7 +211,6 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
     const int step = p.step_ctr ? *p.step_ctr : p.step;
     const double tv = p.tau[((long long)step * p.R + r) * p.ns + a];
     const auto ctau0 = k.tau(tv);
-    const long long fbase = rf * p.N;  // bit / element base of this field
     long long acc = 0;
     bool big = false;
     if constexpr (sizeof(V) == sizeof(float2)) {
@@ -191,11 +218,11 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
       // patterns; FP64 arithmetic is exactly the two subtractions (the
       // compiler otherwise routes 64-bit register moves through the FP64 pipe).
       const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xs);
-      ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(p.xi) + e0;
+      ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(p.xi) + fbase;
       for (int e = tid; e < nel; e += nthr) {
         V *sp = &sm[sidx(e)];
         ulonglong2 xb = xsb[e];
-        const long long pt = (lf0 << lgL) + e;
+        const long long pt = lineoff(e >> lgL) + (e & (L - 1));
         bool evolve = true;
         if (p.bc) {
           const long long bit = fbase + pt;
@@ -213,7 +240,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
                                                           __longlong_as_double((long long)f32_to_f64bits_int(dre)));
           xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
                                                           __longlong_as_double((long long)f32_to_f64bits_int(dim)));
-          xg[e] = xb;
+          xg[pt] = xb;
         }
         acc += to_fixed_bits(xb.x, big);
         V o;
@@ -225,7 +252,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
       for (int e = tid; e < nel; e += nthr) {
         V *sp = &sm[sidx(e)];
         double2 x = xs[e];
-        const long long pt = (lf0 << lgL) + e;
+        const long long pt = lineoff(e >> lgL) + (e & (L - 1));
         bool evolve = true;
         if (p.bc) {
           const long long bit = fbase + pt;
@@ -235,7 +262,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
           auto ctau = ctau0;
           if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
           tdgl_point(x, *sp, k.cd2, k.asf_pi, k.uq2, k.uq2cd2, ctau, k.inv_n);
-          p.xi[e0 + e] = x;
+          p.xi[fbase + pt] = x;
         }
         acc += to_fixed(x.x, big);
         *sp = from_xi<V>(x);
@@ -252,7 +279,14 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   if (p.flags & Z_FWD) line_fft<-1, LG>(th, lgL, tws, line, act);
   if (p.flags & Z_STORE) {
     __syncthreads();
-    for (int e = tid; e < nel; e += nthr) S[e0 + e] = sm[sidx(e)];
+    if (xf) {
+      for (int e = tid; e < nel; e += nthr) {
+        const int t = e & (TL - 1), k = e >> p.lgTL;
+        *sg(t, k) = sm[t * P + k];
+      }
+    } else {
+      for (int e = tid; e < nel; e += nthr) *sg(e >> lgL, e & (L - 1)) = sm[sidx(e)];
+    }
   }
 }
 
@@ -360,11 +394,11 @@ __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, 
 // Fused x-pass on a tile of T consecutive inner indices, all N1 x-values and
 // all NS fields of one replica: forward FFT along x, k-space contraction
 // S[a](k) <- sum_b B_ab(k) S[b](k) (F:4609-4629, b ascending), inverse FFT
-// along x.  Shared memory: twiddles [L] | tile [a][t][x] (x contiguous, odd
-// line pitch) | B tile [P][T*L].  With a compile-time line length the lines
-// come from global memory straight into registers and the inverse FFT's last
-// stage writes them straight back (shared memory only between stages); the B
-// tile streams in by TMA bulk copies during the forward FFT.  One point per thread
+// along x.  S is in the x-fastest layout ([a][y][z][x] per replica), so every
+// line of the tile is L contiguous values.  Shared memory: twiddles [L] | tile
+// [a][t][x] (odd line pitch) | B tile [P][T*L].  The lines arrive by cp.async
+// (whole 128-byte lines per warp), the B tile by TMA bulk copies that stream in
+// during the forward FFT.  One point per thread
 // in the contraction; IN_REGS keeps its NS inputs in registers (FP32, up to
 // 384 threads); FP64 reads them from shared memory and runs at most 256 threads.
 // BFLY (FP32 only): B_ab(k) = (E_ab - u_a . t_b) / mu with t_b = sigma_b f and
@@ -391,20 +425,17 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nel = (NS * L) << lgT;
   auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + x; };
-  // line (a, t) of the tile in global memory: element x at gline(a, t)[x * inner]
-  auto gline = [&](int a, int t) { return S + ((long long)r * NS + a) * L * p.inner + c0 + t; };
   const int E = L >= 8 ? 8 : L, team = L / E, teams = nthr / team;
   const int lines = NS << lgT;
   const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
-  constexpr bool kDirect = LG >= 3;  // compile-time line length: lines go global <-> registers
-  if constexpr (!kDirect) {
-    // S tile: e -> (a, x, t) with t fastest (contiguous in memory)
-    for (int e = tid; e < nel; e += nthr) {
-      const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
-      cp_async_elem(&sm[sidx(a, t, x)], &S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t]);
-    }
-    cp_async_commit();
+  // S is x-fastest: line (a, t) of the tile is L contiguous values; consecutive
+  // lanes copy consecutive x (whole 128-byte lines per warp)
+  auto gline = [&](int ln) { return S + (((long long)r * NS + (ln >> lgT)) * p.inner + c0 + (ln & (TT - 1))) * L; };
+  for (int e = tid; e < nel; e += nthr) {
+    const int x = e & (L - 1), ln = e >> lgL;
+    cp_async_elem(&sm[ln * LP + x], gline(ln) + x);
   }
+  cp_async_commit();
   // B tile: one contiguous block of P * npt values, TMA bulk copies issued by
   // one thread so it streams in during the forward FFT
   __shared__ __align__(8) uint64_t bbar;
@@ -417,27 +448,11 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   if (!BFLY && !bulk)
     for (int i = tid; i < P * npt; i += nthr) Bs[i] = Bt[i];
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
-  if constexpr (kDirect) {
-    constexpr int L8 = 1 << (LG - 3);
-    for (int l0 = 0; l0 < lines; l0 += teams) {
-      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-      const bool act = ln < lines;
-      V v[8];
-      if (act) {
-        const V *g = gline(a, t);
-#pragma unroll
-        for (int m = 0; m < 8; ++m) v[m] = g[(long long)(th + m * L8) * p.inner];
-      }
-      auto line = [&](int l) { return &sm[sidx(a, t, l)]; };
-      line_fft_io<-1, LG, true, false>(v, th, tws, line, line, act);
-    }
-  } else {
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int l0 = 0; l0 < lines; l0 += teams) {
-      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-      line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
-    }
+  cp_async_wait<0>();
+  __syncthreads();
+  for (int l0 = 0; l0 < lines; l0 += teams) {
+    const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+    line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
   }
   if (bulk) mbar_wait(&bbar, 0, p.err);
   __syncthreads();
@@ -512,24 +527,14 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
     for (int a = 0; a < NS; ++a) sm[sidx(a, t, x)] = out[a];
   }
   __syncthreads();
-  if constexpr (kDirect) {
-    for (int l0 = 0; l0 < lines; l0 += teams) {
-      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-      V v[8];
-      V *g = gline(a, t);
-      line_fft_io<+1, LG, false, true>(v, th, tws, [&](int l) { return &sm[sidx(a, t, l)]; },
-                                       [&](int l) { return &g[(long long)l * p.inner]; }, ln < lines);
-    }
-  } else {
-    for (int l0 = 0; l0 < lines; l0 += teams) {
-      const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-      line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
-    }
-    __syncthreads();
-    for (int e = tid; e < nel; e += nthr) {
-      const int t = e & (TT - 1), ax = e >> lgT, x = ax & (L - 1), a = ax >> lgL;
-      S[(((long long)r * NS + a) * L + x) * p.inner + c0 + t] = sm[sidx(a, t, x)];
-    }
+  for (int l0 = 0; l0 < lines; l0 += teams) {
+    const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
+    line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+  }
+  __syncthreads();
+  for (int e = tid; e < nel; e += nthr) {
+    const int x = e & (L - 1), ln = e >> lgL;
+    gline(ln)[x] = sm[ln * LP + x];
   }
 }
 

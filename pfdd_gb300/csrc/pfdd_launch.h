@@ -39,6 +39,9 @@ inline int ilog2(long long v) {
 }
 
 struct Geometry {
+  // spectral layout of a context's S: x fastest ([y][z][x] per field); the
+  // FFT-boundary plans keep the natural [x][y][z]
+  bool xfast = false;
   // z-pass
   int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0;
   size_t zSmem = 0;
@@ -93,12 +96,13 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
 // value, 0 when the x-pass evaluates B(k) itself.  The strided and x-pass tile
 // widths chosen here are the defaults; a context's first step may retune them
 // (they do not change any result).
-inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize) {
+inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, bool xfast = false) {
   Geometry g;
+  g.xfast = xfast;
   const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
   const long long lines = (long long)n1 * n2;
   int TL = std::max(1, kThreads / team3);
-  while ((long long)TL > lines) TL >>= 1;
+  while ((long long)TL > lines || (xfast && TL > n1)) TL >>= 1;  // x-fastest: a block's lines share y
   g.zTL = TL;
   g.zThreads = TL * team3;
   g.zPitch = line_pitch(L3);
@@ -107,7 +111,7 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
   g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
   g.lgL3 = ilog2(L3);
   const int Ls[2] = {n2, n1};
-  const long long inner[2] = {(long long)n3, (long long)n2 * n3};
+  const long long inner[2] = {xfast ? (long long)n3 * n1 : (long long)n3, (long long)n2 * n3};
   for (int ax = 0; ax < 2; ++ax) {
     const int L = Ls[ax], E = std::min(8, L), team = L / E;
     int TI = std::max(1, kThreads / team);

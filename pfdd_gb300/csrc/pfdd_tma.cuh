@@ -59,6 +59,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, int *e
 }
 
 // One thread: copies `bytes` (multiple of 16, both addresses 16-byte aligned)
+// completing on `bar` without raising its expected byte count (the caller
+// announced the total of all its copies with one mbar_arrive_expect_tx).
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  for (unsigned off = 0; off < bytes; off += kBulkChunk) {
+    const unsigned n = bytes - off < kBulkChunk ? bytes - off : kBulkChunk;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32((const char *)dst + off)),
+        "l"((const char *)src + off), "r"(n), "r"(smem_u32(bar))
+        : "memory");
+  }
+}
+
+// One thread: copies `bytes` (multiple of 16, both addresses 16-byte aligned)
 // in chunks, all completing on `bar`, whose expected byte count it raises.
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
   mbar_arrive_expect_tx(bar, bytes);
