@@ -146,7 +146,9 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ long long red[32];
-  const int L = p.L, lgL = p.lgL, TL = p.TL, P = p.pitch;
+  static_assert(LG >= 0, "the z-pass is instantiated per line length");
+  constexpr int L = 1 << LG, lgL = LG;
+  const int TL = p.TL, P = p.pitch;
   V *tws = reinterpret_cast<V *>(smraw);
   V *sm = tws + L;
   double2 *xs = reinterpret_cast<double2 *>(smraw + ((((size_t)L + (size_t)TL * P) * sizeof(V) + 15) & ~(size_t)15));
@@ -155,46 +157,45 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   const long long rf = line0 / p.lines_per_field;
   const int r = (int)(rf / p.ns), a = (int)(rf % p.ns);
   if (p.active && !p.active[r]) return;
-  const long long lf0 = line0 - rf * p.lines_per_field;
+  const int lf0 = (int)(line0 - rf * p.lines_per_field);
   const bool xf = p.sxf != 0;
   // block within the field -> (x block, y) for the x-fastest layout (x block fastest)
   const int xblocks = xf ? p.n1 >> p.lgTL : 1;
-  const int bf = (int)(lf0 / TL);
+  const int bf = lf0 / TL;
   const int x0 = xf ? (bf % xblocks) * TL : 0, yj = xf ? bf / xblocks : 0;
-  // element offset of line t within the field (xi layout, natural)
-  auto lineoff = [&](int t) -> long long { return xf ? ((long long)(x0 + t) * p.n2 + yj) * L : (lf0 + t) * L; };
+  // field-relative offsets (< 2^31): xi element (line t, z = k) at lb + t*ls + k,
+  // S element at sb + t*st + k*sk
+  const int lb = xf ? (x0 * p.n2 + yj) * L : lf0 * L, ls = xf ? p.n2 * L : L;
+  const int sb = xf ? yj * L * p.n1 + x0 : lf0 * L, st = xf ? 1 : L, sk = xf ? p.n1 : 1;
   const long long fbase = rf * p.N;  // element / bit base of this field
   const int nel = TL << lgL;
   const int tid = threadIdx.x, nthr = blockDim.x;
-  V *S = reinterpret_cast<V *>(p.S);
+  V *Sf = reinterpret_cast<V *>(p.S) + fbase;
+  double2 *xif = p.xi + fbase;
   const bool upd = (p.flags & Z_UPDATE) != 0;
   auto sidx = [&](int e) { return (e >> lgL) * P + (e & (L - 1)); };
-  // S element (line t, z = k) in global memory
-  auto sg = [&](int t, int k) -> V * {
-    return xf ? &S[fbase + ((long long)yj * L + k) * p.n1 + x0 + t] : &S[fbase + (lf0 + t) * L + k];
-  };
 
   __shared__ __align__(8) uint64_t xbar;  // completion of the FP64 state tile
   if (upd && tid == 0) {  // TMA bulk copies: one block (natural) or one per line
     mbar_init(&xbar, 1);
     mbar_arrive_expect_tx(&xbar, (unsigned)nel * 16u);
     if (xf)
-      for (int t = 0; t < TL; ++t) bulk_copy(xs + (t << lgL), p.xi + fbase + lineoff(t), (unsigned)L * 16u, &xbar);
+      for (int t = 0; t < TL; ++t) bulk_copy(xs + (t << lgL), xif + lb + t * ls, (unsigned)L * 16u, &xbar);
     else
-      bulk_copy(xs, p.xi + fbase + lf0 * L, (unsigned)nel * 16u, &xbar);
+      bulk_copy(xs, xif + lb, (unsigned)nel * 16u, &xbar);
   }
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   if (p.flags & Z_SRC_XI) {
     for (int e = tid; e < nel; e += nthr)
-      sm[sidx(e)] = from_xi<V>(p.xi[fbase + lineoff(e >> lgL) + (e & (L - 1))]);
+      sm[sidx(e)] = from_xi<V>(xif[lb + (e >> lgL) * ls + (e & (L - 1))]);
   } else if (xf) {
     // consecutive lanes on consecutive x: TL-element runs in global memory
     for (int e = tid; e < nel; e += nthr) {
       const int t = e & (TL - 1), k = e >> p.lgTL;
-      cp_async_elem(&sm[t * P + k], sg(t, k));
+      cp_async_elem(&sm[t * P + k], &Sf[sb + t + k * sk]);
     }
   } else {
-    for (int e = tid; e < nel; e += nthr) cp_async_elem(&sm[sidx(e)], sg(e >> lgL, e & (L - 1)));
+    for (int e = tid; e < nel; e += nthr) cp_async_elem(&sm[sidx(e)], &Sf[sb + e]);
   }
   cp_async_commit();
   cp_async_wait<0>();
@@ -218,11 +219,11 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
       // patterns; FP64 arithmetic is exactly the two subtractions (the
       // compiler otherwise routes 64-bit register moves through the FP64 pipe).
       const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xs);
-      ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(p.xi) + fbase;
+      ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(xif);
       for (int e = tid; e < nel; e += nthr) {
         V *sp = &sm[sidx(e)];
         ulonglong2 xb = xsb[e];
-        const long long pt = lineoff(e >> lgL) + (e & (L - 1));
+        const int pt = lb + (e >> lgL) * ls + (e & (L - 1));
         bool evolve = true;
         if (p.bc) {
           const long long bit = fbase + pt;
@@ -252,7 +253,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
       for (int e = tid; e < nel; e += nthr) {
         V *sp = &sm[sidx(e)];
         double2 x = xs[e];
-        const long long pt = lineoff(e >> lgL) + (e & (L - 1));
+        const int pt = lb + (e >> lgL) * ls + (e & (L - 1));
         bool evolve = true;
         if (p.bc) {
           const long long bit = fbase + pt;
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
           auto ctau = ctau0;
           if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
           tdgl_point(x, *sp, k.cd2, k.asf_pi, k.uq2, k.uq2cd2, ctau, k.inv_n);
-          p.xi[fbase + pt] = x;
+          xif[pt] = x;
         }
         acc += to_fixed(x.x, big);
         *sp = from_xi<V>(x);
@@ -282,10 +283,10 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
     if (xf) {
       for (int e = tid; e < nel; e += nthr) {
         const int t = e & (TL - 1), k = e >> p.lgTL;
-        *sg(t, k) = sm[t * P + k];
+        Sf[sb + t + k * sk] = sm[t * P + k];
       }
     } else {
-      for (int e = tid; e < nel; e += nthr) *sg(e >> lgL, e & (L - 1)) = sm[sidx(e)];
+      for (int e = tid; e < nel; e += nthr) Sf[sb + e] = sm[sidx(e)];
     }
   }
 }
