@@ -137,12 +137,13 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *red) 
 
 // z-pass: TL lines of length L along z (one field), see ZFlags.
 // Shared memory: twiddles [L] | S lines [TL][pitch] (odd pitch) | xi tile
-// [TL][L] double2 (update only).  The S lines arrive by cp.async, the FP64 xi
-// lines by TMA bulk copies that overlap the inverse FFT.  Natural layout: the
-// block's lines are consecutive (x, y) pairs; x-fastest S layout (sxf): the
-// lines (x0 + t, y) of one y, whose S values sit TL to a contiguous run.
+// [TL][L] double2 (update only).  The FP64 xi lines arrive by TMA bulk copies
+// that overlap the inverse FFT.  Natural layout: the block's lines are
+// consecutive (x, y) pairs, whose S values arrive by cp.async; x-fastest S
+// layout (sxf): the lines (x0 + t, y) of one y, whose S values sit TL to a
+// contiguous run and go straight between global memory and registers.
 template <typename T, int LG>
-__global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZParams p) {
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ long long red[32];
@@ -185,9 +186,16 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
       bulk_copy(xs, xif + lb, (unsigned)nel * 16u, &xbar);
   }
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  // x-fastest layout with a forward transform that ends in the store: the S
+  // lines go global <-> registers (consecutive lanes on consecutive x, so every
+  // access covers whole TL-element runs), shared memory only between stages
+  constexpr bool kIO = LG >= 3;
+  const bool direct = kIO && xf && (p.flags & Z_FWD) && (p.flags & Z_STORE);
   if (p.flags & Z_SRC_XI) {
     for (int e = tid; e < nel; e += nthr)
       sm[sidx(e)] = from_xi<V>(xif[lb + (e >> lgL) * ls + (e & (L - 1))]);
+  } else if (direct) {
+    // (the inverse transform loads its input itself)
   } else if (xf) {
     // consecutive lanes on consecutive x: TL-element runs in global memory
     for (int e = tid; e < nel; e += nthr) {
@@ -203,7 +211,24 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
   const int t = tid % TL, th = tid / TL;  // consecutive lanes on consecutive lines
   const bool act = th < team;
   auto line = [&](int l) { return &sm[t * P + l]; };
-  if (p.flags & Z_INV) line_fft<+1, LG>(th, lgL, tws, line, act);
+  auto gline = [&](int l) { return &Sf[sb + t + l * sk]; };  // S element z = l of line t
+  V v[8];
+  if (p.flags & Z_INV) {
+    if constexpr (kIO) {
+      if (direct && !(p.flags & Z_SRC_XI)) {
+        constexpr int L8 = L >> 3;
+        if (act) {
+#pragma unroll
+          for (int m = 0; m < 8; ++m) v[m] = *gline(th + m * L8);
+        }
+        line_fft_io<+1, LG, true, false>(v, th, tws, line, line, act);
+      } else {
+        line_fft<+1, LG>(th, lgL, tws, line, act);
+      }
+    } else {
+      line_fft<+1, LG>(th, lgL, tws, line, act);
+    }
+  }
 
   if (upd) {
     mbar_wait(&xbar, 0, p.err);
@@ -277,6 +302,12 @@ __global__ void __launch_bounds__(256) zpass_kernel(ZParams p) {
     __syncthreads();
   }
 
+  if constexpr (kIO) {
+    if (direct) {  // forward transform, last stage straight to S
+      line_fft_io<-1, LG, false, true>(v, th, tws, line, gline, act);
+      return;
+    }
+  }
   if (p.flags & Z_FWD) line_fft<-1, LG>(th, lgL, tws, line, act);
   if (p.flags & Z_STORE) {
     __syncthreads();
