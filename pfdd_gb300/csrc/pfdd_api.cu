@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -25,22 +26,52 @@ namespace pfdd {
 
 // Deterministic second stage of the gamma sums: one block per (step, replica),
 // fixed-shape tree over the partials of each system.
-__global__ void __launch_bounds__(256) gamma_reduce_kernel(const double *part, int nparts, int R, int ns,
-                                                           double inv_n, double *gamma_a, double *gamma) {
-  __shared__ double red[32];
+__global__ void fill_u64_kernel(unsigned long long *p, long long n, unsigned long long v) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+// Exact sums of the z-pass's fixed-point partials (units of 2^-44) per
+// (step, replica): 128-bit integer accumulation, so gamma_a and gamma do not
+// depend on how the points were split into blocks; one conversion at the end.
+__device__ __forceinline__ double i128_to_double(__int128 v) {
+  const bool neg = v < 0;
+  const unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const double d = (double)(unsigned long long)(u >> 64) * 18446744073709551616.0 + (double)(unsigned long long)u;
+  return neg ? -d : d;
+}
+
+__global__ void __launch_bounds__(256) gamma_reduce_kernel(const long long *part, int nparts, int R, int ns,
+                                                           double scale, double *gamma_a, double *gamma) {
+  __shared__ __int128 red[256];
   const int s = blockIdx.x / R, r = blockIdx.x - s * R;
-  double tot = 0.0;
+  __int128 tot = 0;
+  int totbad = 0;
   for (int a = 0; a < ns; ++a) {
-    const double *pp = part + ((long long)s * R * ns + (long long)r * ns + a) * nparts;
-    double acc = 0.0;
-    for (int c = threadIdx.x; c < nparts; c += blockDim.x) acc += pp[c];
-    const double sum = block_sum(acc, red);
-    if (threadIdx.x == 0) {
-      gamma_a[((long long)s * R + r) * ns + a] = sum * inv_n;
-      tot += sum;
+    const long long *pp = part + ((long long)s * R * ns + (long long)r * ns + a) * nparts;
+    __int128 acc = 0;
+    int bad = 0;
+    for (int c = threadIdx.x; c < nparts; c += blockDim.x) {
+      const long long v = pp[c];
+      if (v == LLONG_MIN) bad = 1;
+      else acc += v;
     }
+    red[threadIdx.x] = acc;
+    bad = __syncthreads_or(bad);
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      gamma_a[((long long)s * R + r) * ns + a] = bad ? __longlong_as_double(0x7ff8000000000000ll)
+                                                     : i128_to_double(red[0]) * scale;
+      tot += red[0];
+      totbad |= bad;
+    }
+    __syncthreads();
   }
-  if (threadIdx.x == 0) gamma[blockIdx.x] = tot * inv_n;
+  if (threadIdx.x == 0)
+    gamma[blockIdx.x] = totbad ? __longlong_as_double(0x7ff8000000000000ll) : i128_to_double(tot) * scale;
 }
 
 // B(k) of Bmatrix (F:328-412) in closed form:
@@ -189,7 +220,8 @@ struct pfdd_ctx {
   double2 *xi = nullptr;
   uint32_t *bc = nullptr;
   void *B = nullptr;
-  double *tau = nullptr, *part = nullptr, *gam_a = nullptr, *gam = nullptr;
+  double *tau = nullptr, *gam_a = nullptr, *gam = nullptr;
+  long long *part = nullptr;  // fixed-point gamma partials
   double *tau_field = nullptr, *dslip_dev = nullptr;
   uint8_t *active = nullptr;
   int *flag = nullptr, *errflag = nullptr, *h_errflag = nullptr;
@@ -215,6 +247,7 @@ struct pfdd_ctx {
   bool primed = false, use_graphs = true;
   // launch plan: tile widths timed on the first step (autotune), as JSON
   bool tuned = false, tune = true;
+  int zparts_cap = 0;  // z-pass blocks per field the partial buffer holds
   std::string plan;
 };
 
@@ -358,10 +391,12 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   if (const char *g = std::getenv("PFDD_NO_TUNE")) c->tune = g[0] == '\0' || g[0] == '0';
   CK(c, cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st));
   CK(c, cudaMallocHost(&c->h_errflag, sizeof(int)));
-  // partial sums for a chunk of steps, bounded to ~32 MB
-  const size_t per_step = RF * (size_t)c->g.zNparts;
-  c->kchunk = (int)std::max<size_t>(1, std::min<size_t>(1024, (4u << 20) / std::max<size_t>(per_step, 1)));
-  CK(c, cudaMalloc(&c->part, per_step * c->kchunk * sizeof(double)));
+  // partial sums for a chunk of steps, bounded to ~32 MB; sized for the
+  // smallest z-pass block the autotuner may pick (a quarter of the default)
+  c->zparts_cap = (int)std::min<long long>((long long)n1 * n2, (long long)c->g.zNparts * 4);
+  const size_t per_step = RF * (size_t)c->zparts_cap;
+  c->kchunk = (int)std::max<size_t>(1, std::min<size_t>(1024, (4u << 20) / per_step));
+  CK(c, cudaMalloc(&c->part, per_step * c->kchunk * sizeof(long long)));
   CK(c, cudaMalloc(&c->tau, (size_t)c->kchunk * RF * sizeof(double)));
   CK(c, cudaMalloc(&c->gam_a, (size_t)c->kchunk * RF * sizeof(double)));
   CK(c, cudaMalloc(&c->gam, (size_t)c->kchunk * nrep * sizeof(double)));
@@ -661,6 +696,31 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
 
 constexpr int kGraphSteps = 16;
 
+// z-pass arguments of a step of this context (the step index comes from the
+// device counter that the x-pass advances)
+static ZParams make_zparams(const pfdd_ctx *c) {
+  ZParams zp;
+  std::memset(&zp, 0, sizeof zp);
+  zp.S = c->S; zp.xi = c->xi; zp.bc = c->anyBc ? c->bc : nullptr; zp.tau = c->tau; zp.tau_field = c->tau_field;
+  zp.dslip = c->dslip_dev; zp.part = c->part; zp.err = c->errflag;
+  zp.active = c->active;
+  zp.step_ctr = c->step_ctr;
+  zp.tw = c->tw[2];
+  zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
+  zp.L = c->n[2]; zp.lgL = c->g.lgL3; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
+  zp.pitch = c->g.zPitch;
+  zp.sxf = c->g.xfast ? 1 : 0;
+  zp.n1 = c->n[0]; zp.n2 = c->n[1]; zp.lgTL = ilog2(c->g.zTL);
+  zp.inv_n = 1.0 / (double)c->N;  // N is a power of two: exact, same as dividing by nsize
+  zp.uq2 = c->uq2;
+  for (int a = 0; a < c->ns; ++a) {
+    zp.cd2[a] = c->cd2[a];
+    zp.asf_pi[a] = c->asf[a] * kPiTrunc;  // Asf2[isa]*pi, F:3488
+    zp.uq2cd2[a] = c->uq2 * c->cd2[a];    // uq2*CD2[isa], F:3489
+  }
+  return zp;
+}
+
 static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   const Geometry &g = c->g;
   char b[768];
@@ -702,10 +762,31 @@ static pfdd_status autotune(pfdd_ctx *c) {
       cudaEventElapsedTime(&ms, e0, e1);
       return 1e3 * ms / 3.0;
     };
-    std::string xs, ys;
+    std::string xs, ys, zs;
     const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
     Geometry best = c->g;
     double bt = 1e30;
+    // z-pass lines per block (the gamma partials are exact integer sums, so
+    // the split of points into blocks changes no result); a typical state
+    // (0.5) and zero stresses so the update takes its usual path
+    fill_u64_kernel<<<1216, kThreads, 0, c->st>>>(reinterpret_cast<unsigned long long *>(c->xi),
+                                                  (long long)c->nrep * c->ns * c->N * 2, 0x3fe0000000000000ull);
+    cudaMemsetAsync(c->tau, 0, (size_t)c->nrep * c->ns * sizeof(double), c->st);
+    for (int lgTL = 0; lgTL <= 5; ++lgTL) {
+      Geometry g = c->g;
+      if (!set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, 1 << lgTL) || g.zNparts > c->zparts_cap) continue;
+      c->g = g;
+      ZParams zp = make_zparams(c);
+      zp.step_ctr = nullptr;
+      zp.step = 0;
+      const double us = time_us([&] { return ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE); });
+      if (us > 0 && us < bt) { bt = us; best = g; }
+      char b[64];
+      snprintf(b, sizeof b, "%s\"%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, us);
+      zs += b;
+    }
+    c->g = best;
+    bt = 1e30;
     for (int lgT = 0; lgT <= 6; ++lgT) {
       Geometry g = c->g;
       if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT)) continue;
@@ -737,7 +818,9 @@ static pfdd_status autotune(pfdd_ctx *c) {
     c->tm.on = timing;
     c->specValid = false;
     c->gen++;  // captured launch shapes change
-    tuning = "{\"x_pass_us_by_tile\": {" + xs + "}, \"y_pass_us_by_tile\": {" + ys + "}}";
+    tuning = "{\"z_pass_us_by_lines\": {" + zs + "}, \"x_pass_us_by_tile\": {" + xs + "}, \"y_pass_us_by_tile\": {" +
+             ys + "}}";
+    cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }
   c->plan = plan_json(c, tuning);
   return PFDD_OK;
@@ -770,25 +853,7 @@ static cudaError_t capture_steps(pfdd_ctx *c, ZParams &zp, int steps, cudaGraphE
 
 template <typename T>
 static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double *gamma, double *gamma_a) {
-  ZParams zp;
-  std::memset(&zp, 0, sizeof zp);
-  zp.S = c->S; zp.xi = c->xi; zp.bc = c->anyBc ? c->bc : nullptr; zp.tau = c->tau; zp.tau_field = c->tau_field;
-  zp.dslip = c->dslip_dev; zp.part = c->part; zp.err = c->errflag;
-  zp.active = c->active;
-  zp.step_ctr = c->step_ctr;
-  zp.tw = c->tw[2];
-  zp.N = c->N; zp.lines_per_field = (long long)c->n[0] * c->n[1];
-  zp.L = c->n[2]; zp.lgL = c->g.lgL3; zp.ns = c->ns; zp.R = c->nrep; zp.TL = c->g.zTL; zp.nparts = c->g.zNparts;
-  zp.pitch = c->g.zPitch;
-  zp.sxf = c->g.xfast ? 1 : 0;
-  zp.n1 = c->n[0]; zp.n2 = c->n[1]; zp.lgTL = ilog2(c->g.zTL);
-  zp.inv_n = 1.0 / (double)c->N;  // N is a power of two: exact, same as dividing by nsize
-  zp.uq2 = c->uq2;
-  for (int a = 0; a < c->ns; ++a) {
-    zp.cd2[a] = c->cd2[a];
-    zp.asf_pi[a] = c->asf[a] * kPiTrunc;  // Asf2[isa]*pi, F:3488
-    zp.uq2cd2[a] = c->uq2 * c->cd2[a];    // uq2*CD2[isa], F:3489
-  }
+  ZParams zp = make_zparams(c);
   const int RF = c->nrep * c->ns;
   if (!c->specValid) {
     CK(c, ctx_zpass(c, zp, Z_SRC_XI | Z_FWD | Z_STORE));
@@ -836,8 +901,8 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
     }
     const int nt = ks * c->nrep;
     t_begin(c);
-    gamma_reduce_kernel<<<nt, kThreads, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, zp.inv_n, c->gam_a,
-                                                    c->gam);
+    gamma_reduce_kernel<<<nt, kThreads, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, 0x1p-44 * zp.inv_n,
+                                                    c->gam_a, c->gam);
     t_end(c, K_GAMMA);
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(c->h_gam_a, c->gam_a, (size_t)ks * RF * sizeof(double), cudaMemcpyDeviceToHost, c->st));

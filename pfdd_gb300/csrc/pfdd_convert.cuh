@@ -102,4 +102,30 @@ PFDD_HD float f64bits_to_f32_int(uint64_t u) {
 // binary64 -> binary32, round to nearest even
 PFDD_HD float f64_to_f32_int(double d) { return f64bits_to_f32_int(f64_bits(d)); }
 
+// The same two conversions on 32-bit words, with a short path for the common
+// case (a binary32-normal result) and the general functions above otherwise.
+// Results are identical to f64bits_to_f32_int / f32_to_f64bits_int.
+PFDD_HD float f64bits_to_f32_fast(uint64_t u) {
+  const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
+  const uint32_t mhi = hi & 0x7fffffffu;
+  // binary64 exponents 897..1150 give binary32 exponents 1..254
+  if (mhi - (897u << 20) < (254u << 20)) {
+    uint32_t v = ((mhi - (896u << 20)) << 3) | (lo >> 29);  // exponent and 23 mantissa bits
+    const uint32_t rem = lo & 0x1fffffffu;                   // the 29 dropped bits
+    v += (uint32_t)(rem > 0x10000000u) | ((uint32_t)(rem == 0x10000000u) & v);  // ties to even
+    return bits_f32(v | (hi & 0x80000000u));
+  }
+  return f64bits_to_f32_int(u);
+}
+
+PFDD_HD uint64_t f32_to_f64bits_fast(float f) {
+  const uint32_t u = f32_bits(f);
+  const uint32_t e8 = (u >> 23) & 0xffu;
+  if (e8 == 0xffu) return f32_to_f64bits_int(f);
+  const uint32_t sign = u & 0x80000000u;
+  const uint32_t hi = e8 ? sign | (((u & 0x7fffffffu) >> 3) + (896u << 20)) : sign;
+  const uint32_t lo = e8 ? u << 29 : 0u;
+  return ((uint64_t)hi << 32) | lo;
+}
+
 }  // namespace pfdd

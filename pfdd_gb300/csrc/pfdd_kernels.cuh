@@ -15,6 +15,9 @@
 //   z-forward FFT of the new state).
 // S therefore holds the z-transformed state between steps.
 #pragma once
+#include <climits>
+#include <type_traits>
+
 #include "pfdd_convert.cuh"
 #include "pfdd_fft.cuh"
 #include "pfdd_tma.cuh"
@@ -37,7 +40,7 @@ struct ZParams {
   const double *tau;        // [step][R][ns]: tau/dslip (no field) or ramp multiplier (field)
   const double *tau_field;  // [ns][N] or null
   const double *dslip;      // [ns] (field mode)
-  double *part;             // [step][R*ns][nparts]
+  long long *part;          // [step][R*ns][nparts] exact fixed-point partial sums (LLONG_MIN: overflow)
   const uint8_t *active;    // [R] or null
   const void *tw;           // forward twiddles of length L
   int *err;                 // set when a bounded wait times out (may be null)
@@ -245,35 +248,45 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
       // compiler otherwise routes 64-bit register moves through the FP64 pipe).
       const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xs);
       ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(xif);
-      for (int e = tid; e < nel; e += nthr) {
-        V *sp = &sm[sidx(e)];
-        ulonglong2 xb = xsb[e];
-        const int pt = lb + (e >> lgL) * ls + (e & (L - 1));
-        bool evolve = true;
-        if (p.bc) {
-          const long long bit = fbase + pt;
-          evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
-        }
-        if (evolve) {
+      // general: pinned points or a stress field (read per point); otherwise
+      // every point evolves under the block's one stress value
+      auto update = [&](auto general) {
+        constexpr bool kGeneral = decltype(general)::value;
+#pragma unroll 2
+        for (int e = tid; e < nel; e += nthr) {
+          V *sp = &sm[sidx(e)];
+          ulonglong2 xb = xsb[e];
+          const int pt = lb + (e >> lgL) * ls + (e & (L - 1));
+          bool evolve = true;
           float ctau = ctau0;
-          if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
-          const float2 f = *sp;
-          const float xr = f64bits_to_f32_int(xb.x);
-          const float s = sinpif(2.0f * xr);
-          const float dre = k.cd2 * (k.uq2 * f.x * k.inv_n + k.asf_pi * s - ctau);
-          const float dim = k.uq2cd2 * (f.y * k.inv_n);
-          xb.x = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.x) -
-                                                          __longlong_as_double((long long)f32_to_f64bits_int(dre)));
-          xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
-                                                          __longlong_as_double((long long)f32_to_f64bits_int(dim)));
-          xg[pt] = xb;
+          if constexpr (kGeneral) {
+            if (p.bc) {
+              const long long bit = fbase + pt;
+              evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
+            }
+            if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
+          }
+          if (evolve) {
+            const float2 f = *sp;
+            const float xr = f64bits_to_f32_fast(xb.x);
+            const float s = sinpif(2.0f * xr);
+            const float dre = k.cd2 * (k.uq2 * f.x * k.inv_n + k.asf_pi * s - ctau);
+            const float dim = k.uq2cd2 * (f.y * k.inv_n);
+            xb.x = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.x) -
+                                                            __longlong_as_double((long long)f32_to_f64bits_fast(dre)));
+            xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
+                                                            __longlong_as_double((long long)f32_to_f64bits_fast(dim)));
+            xg[pt] = xb;
+          }
+          acc += to_fixed_bits(xb.x, big);
+          V o;
+          o.x = f64bits_to_f32_fast(xb.x);
+          o.y = f64bits_to_f32_fast(xb.y);
+          *sp = o;
         }
-        acc += to_fixed_bits(xb.x, big);
-        V o;
-        o.x = f64bits_to_f32_int(xb.x);
-        o.y = f64bits_to_f32_int(xb.y);
-        *sp = o;
-      }
+      };
+      if (p.bc || p.tau_field) update(std::true_type{});
+      else update(std::false_type{});
     } else {
       for (int e = tid; e < nel; e += nthr) {
         V *sp = &sm[sidx(e)];
@@ -296,9 +309,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
     }
     const long long s = block_sum_i64(acc, red);
     const int anybig = __syncthreads_or(big);
-    if (tid == 0)
-      p.part[((long long)step * p.R * p.ns + rf) * p.nparts + lf0 / TL] =
-          anybig ? __longlong_as_double(0x7ff8000000000000ll) : (double)s * 0x1p-44;
+    if (tid == 0) p.part[((long long)step * p.R * p.ns + rf) * p.nparts + lf0 / TL] = anybig ? LLONG_MIN : s;
     __syncthreads();
   }
 

@@ -57,6 +57,21 @@ struct Geometry {
 
 inline int line_pitch(int L) { return L + 1; }  // odd pitch: lanes on different lines hit different banks
 
+// z-pass with TL lines per block (the x-fastest layout needs TL <= N1).
+inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, int TL) {
+  const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
+  const long long lines = (long long)n1 * n2;
+  if (TL < 1 || TL > lines || (g.xfast && TL > n1) || (long long)TL * team3 > kThreads) return false;
+  g.zTL = TL;
+  g.zThreads = TL * team3;
+  g.zPitch = line_pitch(L3);
+  g.zNparts = (int)(lines / TL);
+  // twiddles + padded S lines (16-byte aligned) + FP64 xi tile
+  g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
+  g.lgL3 = ilog2(L3);
+  return g.zSmem <= 200 * 1024;
+}
+
 // Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.
 inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, int lgTI, size_t vsize) {
   const int E = std::min(8, L), team = L / E;
@@ -103,13 +118,7 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
   const long long lines = (long long)n1 * n2;
   int TL = std::max(1, kThreads / team3);
   while ((long long)TL > lines || (xfast && TL > n1)) TL >>= 1;  // x-fastest: a block's lines share y
-  g.zTL = TL;
-  g.zThreads = TL * team3;
-  g.zPitch = line_pitch(L3);
-  g.zNparts = (int)(lines / TL);
-  // twiddles + padded S lines (16-byte aligned) + FP64 xi tile
-  g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
-  g.lgL3 = ilog2(L3);
+  set_z_geometry(g, n1, n2, n3, vsize, TL);
   const int Ls[2] = {n2, n1};
   const long long inner[2] = {xfast ? (long long)n3 * n1 : (long long)n3, (long long)n2 * n3};
   for (int ax = 0; ax < 2; ++ax) {

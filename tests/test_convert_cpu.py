@@ -14,6 +14,7 @@ HARNESS = r"""
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
+#include <initializer_list>
 #include <random>
 #include "pfdd_convert.cuh"
 using namespace pfdd;
@@ -63,7 +64,21 @@ int main() {
   edge += f32_to_f64_int(1e-45f) != 0.0;  // subnormal input flushes
   edge += f64_to_f32_int((double)FLT_MAX) != FLT_MAX;
   edge += f64_to_f32_int(1.0 + 1e-9) != 1.0f;
-  printf("%ld %ld %d\n", checked, bad, edge);
+  // the 32-bit-word short paths agree with the general functions on every
+  // pattern class (random bits across all exponents, ties, zeros, Inf/NaN)
+  long fastbad = 0;
+  for (int i = 0; i < 1000000; ++i) {
+    uint64_t u = rng();
+    if (i % 3 == 0) u = (u & ~0x7ff0000000000000ull) | ((uint64_t)(880 + rng() % 290) << 52);
+    if (i % 7 == 0) u = (u & ~0x1fffffffull) | (1ull << 28);
+    if (fb(f64bits_to_f32_fast(u)) != fb(f64bits_to_f32_int(u))) ++fastbad;
+    uint32_t w = (uint32_t)rng();
+    if (f32_to_f64bits_fast(mkf(w)) != f32_to_f64bits_int(mkf(w))) ++fastbad;
+  }
+  for (uint64_t u : std::initializer_list<uint64_t>{0ull, 1ull << 63, 0x7ff0000000000000ull, 0xfff8000000000001ull,
+                                                    db(FLT_MAX), db(FLT_MIN), db((double)FLT_MAX * (1 + 1e-9)), db(1.0)})
+    if (fb(f64bits_to_f32_fast(u)) != fb(f64bits_to_f32_int(u))) ++fastbad;
+  printf("%ld %ld %d %ld\n", checked, bad, edge, fastbad);
   return 0;
 }
 """
@@ -76,7 +91,8 @@ def test_integer_conversions_match_ieee(tmp_path):
     subprocess.run(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "pfdd_gb300" / "csrc"), str(src), "-o", str(exe)],
                    check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
-    checked, bad, edge = map(int, out)
+    checked, bad, edge, fastbad = map(int, out)
     assert checked > 1_500_000
     assert bad == 0
     assert edge == 0
+    assert fastbad == 0
