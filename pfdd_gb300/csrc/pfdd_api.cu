@@ -744,6 +744,30 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
+  // PFDD_PLAN="z=<lines>,x=<tile columns>,y=<tile columns>" pins the plan (each
+  // entry optional, ignored when it does not fit) instead of timing it, e.g.
+  // to profile the plan a timed run chose (a profiler distorts the timings)
+  if (const char *pin = std::getenv("PFDD_PLAN")) {
+    const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
+    for (const char *q = pin; *q;) {
+      char key = 0;
+      int v = 0;
+      if (std::sscanf(q, "%c=%d", &key, &v) == 2 && v > 0) {
+        Geometry g = c->g;
+        const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v) && g.zNparts <= c->zparts_cap
+                        : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v))
+                        : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs)
+                                     : false;
+        if (ok) c->g = g;
+      }
+      const char *comma = std::strchr(q, ',');
+      if (!comma) break;
+      q = comma + 1;
+    }
+    c->gen++;
+    c->plan = plan_json(c, "\"pinned\"");
+    return PFDD_OK;
+  }
   if (c->tune) {
     const bool timing = c->tm.on;
     c->tm.on = false;

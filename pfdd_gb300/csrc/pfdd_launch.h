@@ -57,6 +57,16 @@ struct Geometry {
 
 inline int line_pitch(int L) { return L + 1; }  // odd pitch: lanes on different lines hit different banks
 
+// Pitch of the z-pass lines, whose consecutive lanes walk TL lines and then the
+// next position of the same lines.  A shared-memory phase serves 128 bytes,
+// i.e. u = 128 / vsize lanes; with TL >= u they all sit on different lines and
+// an odd pitch spreads them, with TL < u each line holds u / TL consecutive
+// lanes and a pitch of u / TL (mod u) puts the lines side by side.
+inline int z_line_pitch(int L, int TL, size_t vsize) {
+  const int u = (int)(128 / vsize);
+  return TL >= u ? L + 1 : L + u / TL;
+}
+
 // z-pass with TL lines per block (the x-fastest layout needs TL <= N1).
 inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, int TL) {
   const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
@@ -64,7 +74,7 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   if (TL < 1 || TL > lines || (g.xfast && TL > n1) || (long long)TL * team3 > kThreads) return false;
   g.zTL = TL;
   g.zThreads = TL * team3;
-  g.zPitch = line_pitch(L3);
+  g.zPitch = z_line_pitch(L3, TL, vsize);
   g.zNparts = (int)(lines / TL);
   // twiddles + padded S lines (16-byte aligned) + FP64 xi tile
   g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;

@@ -42,3 +42,18 @@ def test_tuned_plan_gives_same_bits(native_lib, precision):
     assert len(tried) >= 1 and all(v > 0 for v in tried.values())
     assert str(p1["x_pass"]["tile_columns"]) in tried
     assert p1["radix_plan"] == ["8x4", "8x2", "8x8"]
+
+
+def test_pinned_plan(native_lib):
+    spec = workloads.SolveSpec(n=(32, 16, 64), ns=12, steps=6, sigma_max=0.05, noise_seed=22,
+                               loops=workloads.random_loops((32, 16, 64), 3, 2.0, 6.0, 12, seed=22))
+    os.environ["PFDD_PLAN"] = "z=8,x=2,y=8"
+    try:
+        g1, x1, p1 = run(spec, "fp32", True)
+    finally:
+        del os.environ["PFDD_PLAN"]
+    g0, x0, _ = run(spec, "fp32", False)
+    assert p1["autotune"] == "pinned"
+    assert (p1["z_pass"]["lines"], p1["x_pass"]["tile_columns"], p1["y_pass"]["tile_columns"]) == (8, 2, 8)
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(x1, x0)
