@@ -36,6 +36,11 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
                                only); big tables calloc'ed
 11  4672                       extra full-precision per-step log (gamma_full.dat):
                                step, gamma, gamma_a[0..NS-1], wall-clock time
+12  818, 927                   ``PFDD_STRAIN_OUT``: strain.txt / stress.txt of the
+                               state at the start of outer step 1 (the initial xi:
+                               the inner loop runs in that step) plus full-precision
+                               dumps of the strain and stress fields
+                               (eps_full.bin, sigma_full.bin)
 ==  =========================  ====================================================
 """
 from __future__ import annotations
@@ -89,6 +94,11 @@ DEFAULTS_BLOCK = r"""
 #ifndef PFDD_SETUP_B
 #define PFDD_SETUP_B 1
 #endif
+#ifndef PFDD_STRAIN_OUT
+#define PFDD_STRAIN_OUT 0
+#endif
+#define PFDD_DUMP(name_, arr_, n_) do { FILE *f_ = fopen(name_, "wb"); \
+    fwrite((arr_), sizeof(*(arr_)), (size_t)(n_), f_); fclose(f_); } while (0)
 static int pfdd_krun_(int k_) { const char *s_ = getenv("PFDD_KRUN"); return s_ ? atoi(s_) : k_; }
 #define PFDD_LOG_STEP(itp_, g_, g1_) do { static FILE *pfdd_gf_; int q_; \
     if (!pfdd_gf_) pfdd_gf_ = fopen("gamma_full.dat", "w"); \
@@ -109,6 +119,12 @@ PATCHES = [
     (302, "mc->C11=168.4E9;", "mc->C11=2.0*PFDD_MU+PFDD_LAMBDA;"),
     (303, "mc->C12=121.4E9;", "mc->C12=PFDD_LAMBDA;"),
     (304, "mc->C44=23.5E9;", "mc->C44=PFDD_MU;"),
+    (818, "if(it == NT-NTD-1){",
+     "if (PFDD_STRAIN_OUT && it == 1) PFDD_DUMP(\"eps_full.bin\", dataeps, 2*N1*N2*N3*ND*ND);\n"
+     "  if(it == NT-NTD-1 || (PFDD_STRAIN_OUT && it == 1)){"),
+    (927, "if (it == NT-1 && itp == NP-1) {",
+     "if (PFDD_STRAIN_OUT && it == 1) PFDD_DUMP(\"sigma_full.bin\", datasigma, 2*N1*N2*N3*ND*ND);\n"
+     "  if ((it == NT-1 && itp == NP-1 && !PFDD_STRAIN_OUT) || (PFDD_STRAIN_OUT && it == 1)) {"),
     (1432, "if(isa >= NS) {", "if(0) {"),
     (1903, "xb[i][j] = xb[i][j]/2.0;", "xb[i][j] = xb[i][j]/PFDD_BDIV;"),
     (3484, "-tau[i][j][k][isa]/dslip2[isa]", "-tau[i][j][k][isa]*((it_plastic+1.0)/PFDD_K)/dslip2[isa]"),
@@ -169,27 +185,31 @@ def write_patched_source(src: Path = REF_SRC, dst: Path = PATCHED) -> Path:
     return dst
 
 
-def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01) -> str:
+def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01, strain=False) -> str:
     tag = "x".join(str(int(v)) for v in n)
     return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}_{'fp64' if fp64 else 'fp32'}"
-            f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}")
+            f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}{'_strain' if strain else ''}")
 
 
 def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=True,
-                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False) -> Path:
+                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False) -> Path:
+    """strain=True (implies diag): strain.txt, stress.txt and the full-precision
+    strain/stress dumps of the initial state (patch 12)."""
+    diag = diag or strain
     """Compile one configuration of the patched reference; returns the binary path."""
     if REF_SRC.exists() and (force or not PATCHED.exists()
                              or PATCHED.stat().st_mtime < Path(__file__).stat().st_mtime):
         write_patched_source()
     if not PATCHED.exists():
         raise FileNotFoundError("patched reference source missing (no reference checkout here)")
-    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2)
+    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain)
     if out.exists() and out.stat().st_mtime >= PATCHED.stat().st_mtime and not force:
         return out
     defs = [f"-DPFDD_N1={n[0]}", f"-DPFDD_N2={n[1]}", f"-DPFDD_N3={n[2]}", f"-DPFDD_K={k}",
             f"-DPFDD_SIGMA={sigma!r}", f"-DPFDD_ASF={asf!r}", f"-DPFDD_CD2={cd2!r}",
             f"-DPFDD_MU={mu!r}", f"-DPFDD_LAMBDA={lam!r}",
-            f"-DPFDD_DIAG={1 if diag else 0}", f"-DPFDD_SETUP_B={1 if setup_b else 0}"]
+            f"-DPFDD_DIAG={1 if diag else 0}", f"-DPFDD_SETUP_B={1 if setup_b else 0}",
+            f"-DPFDD_STRAIN_OUT={1 if strain else 0}"]
     if fp64:
         defs.append("-Dfloat=double")
     cmd = ["gcc", "-O2", "-w", "-DUSE_FOURN", *defs]

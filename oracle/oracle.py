@@ -46,6 +46,9 @@ def lib():
         L.oracle_resolss_uniform.argtypes = [C.c_int, dp, dp, dp]
         L.oracle_bmatrix.argtypes = [C.c_int] * 3 + [C.c_double] * 6 + [C.c_int, dp, dp, C.c_int]
         L.oracle_fft3d.argtypes = [C.c_int] * 4 + [dp, C.c_int, C.c_int]
+        L.oracle_strain_stress.argtypes = ([C.c_int] * 4 + [C.c_double] * 3 + [dp] + [C.c_double] * 3 +
+                                           [dp, dp, dp, dp, dp, dp, C.c_int])
+        L.oracle_strain_stress.restype = None
         L.oracle_run.argtypes = ([C.c_int] * 4 + [dp, dp, dp, dp, dp, dp, C.c_double, C.c_int, dp,
                                  C.c_void_p, dp, dp, C.c_int])
         L.oracle_run.restype = C.c_int
@@ -137,3 +140,21 @@ def solve(spec, steps: int | None = None, eps_bdiv: float = float(np.sqrt(2.0)))
     xi, bc = workloads.initial_state(spec)
     ns = spec.ns
     return run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf), np.full(ns, spec.dslip), 1.0, tau)
+
+
+def strain_stress(n, xi: np.ndarray, eps: np.ndarray, C11: float, C12: float, C44: float, sigma_app: np.ndarray,
+                  d=(1.0, 1.0, 1.0)):
+    """Strain and stress fields of state ``xi`` (complex [ns, n1, n2, n3]):
+    returns eps [3, 3, N], sigma [3, 3, N], aveps [3, 3], avesigma [3, 3]."""
+    L = lib()
+    n = tuple(int(v) for v in n)
+    N = int(np.prod(n))
+    ns = xi.shape[0]
+    x = np.empty((ns, N, 2))
+    x[..., 0] = xi.reshape(ns, N).real
+    x[..., 1] = xi.reshape(ns, N).imag
+    e = np.ascontiguousarray(eps[:ns], dtype=np.float64)
+    sa = np.ascontiguousarray(sigma_app, dtype=np.float64)
+    eo = np.zeros((9, N)); so = np.zeros((9, N)); ae = np.zeros(9); asg = np.zeros(9)
+    L.oracle_strain_stress(*n, ns, C11, C12, C44, e, *map(float, d), x, sa, eo, so, ae, asg, nthreads())
+    return eo.reshape(3, 3, N), so.reshape(3, 3, N), ae.reshape(3, 3), asg.reshape(3, 3)

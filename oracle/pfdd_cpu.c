@@ -350,3 +350,143 @@ int oracle_run(int n1, int n2, int n3, int ns, const double *B, double *xi, cons
   free(data); free(d2);
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* strain and stress fields of a state (diagnostics, §8f)              */
+
+struct fm_ctx {
+  int n1, n2, n3, ns;
+  const double *fx, *fy, *fz;
+  double mu, ll, mup, C[3][3][3][3];
+  const double (*eps)[3][3];
+  const double *xhat; /* [ns][N][2], forward FFT of xi */
+  double *beta;       /* [9][N][2], component i + 3 j */
+};
+
+/* k-space strain, F:414-598 (F matrix, MT = 1 so C_rotate = C, F:486) and
+ * F:761-778 (databeta = sum_a F_a,ij data_a): F_a,ij = sum_klmn C_klmn G_jk
+ * eps_a,mn f_i f_l, accumulated in the reference's loop order. */
+static void fm_range(void *p, int64_t lo, int64_t hi) {
+  struct fm_ctx *c = (struct fm_ctx *)p;
+  const int64_t N = (int64_t)c->n1 * c->n2 * c->n3;
+  const double mu = c->mu, ll = c->ll, mupc = c->mup;
+  for (int64_t pt = lo; pt < hi; ++pt) {
+    int k3 = (int)(pt % c->n3), k2 = (int)((pt / c->n3) % c->n2), k1 = (int)(pt / ((int64_t)c->n3 * c->n2));
+    double fk[3] = {c->fx[k1], c->fy[k2], c->fz[k3]};
+    double fk2 = fk[0] * fk[0] + fk[1] * fk[1] + fk[2] * fk[2];
+    double F[12][3][3];
+    memset(F, 0, sizeof F);
+    if (fk2 > 0) {
+      /* G of F:538-540 */
+      double z2[3] = {fk[0] * fk[0] / fk2, fk[1] * fk[1] / fk2, fk[2] * fk[2] / fk2};
+      double kk = 1.0 + (mu + ll) * (1 / (mu + mupc * z2[0]) * z2[0] + 1 / (mu + mupc * z2[1]) * z2[1] +
+                                     1 / (mu + mupc * z2[2]) * z2[2]);
+      double G[3][3];
+      for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < 3; ++i)
+          G[k][i] = 1 / fk2 * (DLT(i, k) / (mu + mupc * z2[k]) -
+                               fk[i] * fk[k] / fk2 / (mu + mupc * z2[i]) / (mu + mupc * z2[k]) * (mu + ll) / kk);
+      for (int ka = 0; ka < c->ns; ++ka)
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k)
+              for (int l = 0; l < 3; ++l)
+                for (int m = 0; m < 3; ++m)
+                  for (int n = 0; n < 3; ++n)
+                    F[ka][i][j] = F[ka][i][j] + c->C[k][l][m][n] * G[j][k] * c->eps[ka][m][n] * fk[i] * fk[l];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double re = 0., im = 0.;
+        for (int a = 0; a < c->ns; ++a) {
+          re += c->xhat[2 * ((int64_t)a * N + pt)] * F[a][i][j];
+          im += c->xhat[2 * ((int64_t)a * N + pt) + 1] * F[a][i][j];
+        }
+        c->beta[2 * ((int64_t)(i + 3 * j) * N + pt)] = re;
+        c->beta[2 * ((int64_t)(i + 3 * j) * N + pt) + 1] = im;
+      }
+  }
+}
+
+/* Strain and stress of the state xi ([ns][N][2]) under the uniform applied
+ * stress sig_app[3][3] (units of C44, the reference's sigma array, F:3820-3918):
+ *   avepsd_ij = sum_a eps_a,ij <Re xi_a>                        (avestrain, F:670-688)
+ *   avepst_ij = sum_kl S_ijkl sig_app_kl mu + avepsd_ij          (F:726-741; S of F:661-664
+ *               with S11, S12, S44 of main, F:4261-4263)
+ *   beta_ij   = IFFT(sum_a F_a,ij FFT(xi_a))/N + avepst_ij      (strain, F:761-799)
+ *   eps_ij    = (beta_ij + beta_ji)/2                            (F:801-812)
+ *   sig_ij    = sum_kl C_ijkl (eps_kl - sum_a eps_a,kl Re xi_a)  (stress, F:885-921)
+ *   aveps, avesig: means over the grid                           (F:4063-4072, F:920)
+ * Outputs: eps_out[9][N], sig_out[9][N] (component 3 i + j, real parts),
+ * aveps[9], avesig[9] (3 i + j). */
+void oracle_strain_stress(int n1, int n2, int n3, int ns, double C11, double C12, double C44,
+                          const double (*eps)[3][3], double d1, double d2, double d3, const double *xi,
+                          const double sig_app[3][3], double *eps_out, double *sig_out, double *aveps,
+                          double *avesig, int nthreads) {
+  const int64_t N = (int64_t)n1 * n2 * n3;
+  struct fm_ctx c;
+  c.n1 = n1; c.n2 = n2; c.n3 = n3; c.ns = ns; c.eps = eps;
+  double *fx = (double *)malloc(sizeof(double) * n1), *fy = (double *)malloc(sizeof(double) * n2),
+         *fz = (double *)malloc(sizeof(double) * n3);
+  oracle_frec(n1, d1, fx); oracle_frec(n2, d2, fy); oracle_frec(n3, d3, fz);
+  c.fx = fx; c.fy = fy; c.fz = fz;
+  const double mu = C44, ll = C12, mup = C11 - C12 - 2 * C44;
+  c.mu = mu; c.ll = ll; c.mup = mup;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k)
+        for (int m = 0; m < 3; ++m)
+          c.C[i][j][k][m] = mu * (DLT(i, k) * DLT(j, m) + DLT(i, m) * DLT(j, k)) + ll * DLT(i, j) * DLT(k, m) +
+                            mup * DLT4(i, j, k, m);
+  double *xhat = (double *)malloc(sizeof(double) * 2 * N * ns);
+  memcpy(xhat, xi, sizeof(double) * 2 * N * ns);
+  oracle_fft3d(n1, n2, n3, ns, xhat, -1, nthreads);
+  double *beta = (double *)malloc(sizeof(double) * 2 * N * 9);
+  c.xhat = xhat; c.beta = beta;
+  parallel_for(N, nthreads, fm_range, &c);
+  oracle_fft3d(n1, n2, n3, 9, beta, +1, nthreads);
+  /* compliance of main (F:4261-4263) and S_ijkl of avestrain (F:661-664) */
+  const double S11 = 1. / 3. * (1 / (C11 + 2 * C12) + 2 / (C11 - C12));
+  const double S12 = 1. / 3. * (1 / (C11 + 2 * C12) - 1 / (C11 - C12));
+  const double S44 = 1 / C44;
+  double avepsd[3][3] = {{0}}, avepst[3][3];
+  for (int a = 0; a < ns; ++a)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int64_t pt = 0; pt < N; ++pt) avepsd[i][j] += eps[a][i][j] * xi[2 * ((int64_t)a * N + pt)] / (double)N;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) {
+          const double Sijkl = (S11 + 2 * S12) / 3.0 * DLT(i, j) * DLT(k, l) +
+                               S44 / 4.0 * (DLT(i, k) * DLT(j, l) + DLT(i, l) * DLT(j, k)) - S44 / 2.0 * DLT4(i, j, k, l) +
+                               (S11 - S12) * (DLT4(i, j, k, l) - DLT(i, j) * DLT(k, l) / 3.0);
+          s += Sijkl * sig_app[k][l] * mu;
+        }
+      avepst[i][j] = s + avepsd[i][j];
+    }
+  for (int q = 0; q < 9; ++q) { aveps[q] = 0.; avesig[q] = 0.; }
+  for (int64_t pt = 0; pt < N; ++pt) {
+    double b[3][3], e[3][3], ed[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        b[i][j] = beta[2 * ((int64_t)(i + 3 * j) * N + pt)] / (double)N + avepst[i][j];
+        ed[i][j] = 0.;
+        for (int a = 0; a < ns; ++a) ed[i][j] += eps[a][i][j] * xi[2 * ((int64_t)a * N + pt)];
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) e[i][j] = (b[i][j] + b[j][i]) / 2.;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double s = 0.;
+        for (int k = 0; k < 3; ++k)
+          for (int l = 0; l < 3; ++l) s += c.C[i][j][k][l] * (e[k][l] - ed[k][l]);
+        eps_out[(int64_t)(3 * i + j) * N + pt] = e[i][j];
+        sig_out[(int64_t)(3 * i + j) * N + pt] = s;
+        aveps[3 * i + j] += e[i][j] / (double)N;
+        avesig[3 * i + j] += s / (double)N;
+      }
+  }
+  free(fx); free(fy); free(fz); free(xhat); free(beta);
+}

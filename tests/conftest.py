@@ -25,7 +25,13 @@ def native_lib():
 
 
 def golden_cases():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    """Trajectory cases (gamma per step and final xi of the reference's own run)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("strain_"))
+
+
+def strain_golden_cases():
+    """Strain/stress fields of an initial state, from the reference's own run."""
+    return sorted(p.stem for p in GOLDEN.glob("strain_*.npz"))
 
 
 def load_golden(name):

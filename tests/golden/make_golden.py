@@ -6,7 +6,8 @@ For every case it builds the patched reference (oracle/build_ref.py) in FP64
 spectral precision, writes the seeded inputs as xi.dat / xi_bc.dat (the reference is
 built with 12 FCC systems; systems beyond the case's ``ns`` are zero and pinned), runs
 it, and stores per-step gamma / gamma_a (full precision) and the final xi (full field
-for small grids, a seeded sample of points otherwise) in ``<case>.npz``.
+for small grids, a seeded sample of points otherwise) in ``<case>.npz``.  The
+``strain_*`` cases hold the reference's strain and stress fields of an initial state.
 """
 from __future__ import annotations
 
@@ -96,8 +97,54 @@ def make(name: str, spec: workloads.SolveSpec):
     print(f"{name}: K={K} gamma[-1]={g64[-1, 1]:.6e} fp32-ref max|dxi|={float(out['fp32ref_max_dxi']):.2e}")
 
 
+def strain_cases():
+    """Strain/stress of an initial state (patch 12 of oracle/build_ref.py): the
+    reference dumps both fields in full precision and writes strain.txt,
+    stress.txt and the averages of stress-strain.dat for the state it starts from."""
+    yield "strain_fcc12_8x16x16", workloads.SolveSpec(
+        n=(8, 16, 16), ns=12, steps=2, sigma_max=0.05,
+        loops=workloads.random_loops((8, 16, 16), 4, 2.0, 5.0, 12, seed=31), noise_seed=31)
+    c0 = workloads.config0()
+    c0.steps = 2
+    yield "strain_config0_32c_ns3", c0
+
+
+def make_strain(name: str, spec: workloads.SolveSpec):
+    b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=True, strain=True,
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
+    d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
+    try:
+        xi, bc = workloads.initial_state(spec)
+        refio.write_xi_files(d, xi, bc, ns_ref=12)
+        build_ref.run_ref(b, d)
+        N = spec.npts
+        # dumps: [component i + 3 j][point][re, im]; stored as [3 i + j][point], real parts
+        e = np.fromfile(d / "eps_full.bin").reshape(9, N, 2)[..., 0]
+        s = np.fromfile(d / "sigma_full.bin").reshape(9, N, 2)[..., 0]
+        order = [i + 3 * j for i in range(3) for j in range(3)]
+        e, s = e[order], s[order]
+        ss = np.loadtxt(d / "stress-strain.dat")
+        strain_txt = (d / "strain.txt").read_text().splitlines()
+        stress_txt = (d / "stress.txt").read_text().splitlines()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    out = dict(spec=spec_json(spec), aveps_txt=ss[0:18:2], avesigma_over_mu_txt=ss[1:18:2],
+               strain_txt_head=np.array(strain_txt[:6]), strain_txt_lines=np.array(len(strain_txt)),
+               stress_txt_head=np.array(stress_txt[:6]), stress_txt_lines=np.array(len(stress_txt)))
+    if N <= FULL_LIMIT:
+        out["eps"], out["sigma"] = e, s
+    else:
+        idx = sample_points(N, 2048, seed=777)
+        out["sample_idx"], out["eps_sample"], out["sigma_sample"] = idx, e[:, idx], s[:, idx]
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print(f"{name}: max|eps|={np.abs(e).max():.3e} max|sigma|={np.abs(s).max():.3e}")
+
+
 if __name__ == "__main__":
     want = set(sys.argv[1:])
     for nm, sp in cases():
         if not want or nm in want:
             make(nm, sp)
+    for nm, sp in strain_cases():
+        if not want or nm in want:
+            make_strain(nm, sp)

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, load_golden, strain_golden_cases
 from oracle import oracle
 from pfdd_gb300 import workloads
 
@@ -111,3 +111,33 @@ def test_pinned_points_do_not_move():
     xf, _, _ = oracle.run(spec.n, B, xi, bc, [0.01] * 3, [0.1] * 3, [1.0] * 3, 1.0, tau)
     np.testing.assert_array_equal(xf[1, :4], xi[1, :4])
     assert np.max(np.abs(xf[1, 4:] - xi[1, 4:])) > 0
+
+
+def strain_inputs(spec):
+    """Initial state, eigenstrains, constants and applied stress of a strain golden case."""
+    xi, _ = workloads.initial_state(spec)
+    eps = oracle.fcc_eps(12)[:spec.ns]
+    sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
+    return xi, eps, 2 * spec.mu + spec.lam, spec.lam, spec.mu, sig
+
+
+@pytest.mark.parametrize("name", strain_golden_cases())
+def test_oracle_strain_stress_matches_reference(name):
+    """Strain and stress fields (strain F:752-835, stress F:837-972) of the initial
+    state: the restatement against the reference's own full-precision dump, and its
+    averages against the reference's stress-strain.dat (printed with %e)."""
+    spec, z = load_golden(name)
+    xi, eps, C11, C12, C44, sig = strain_inputs(spec)
+    e, s, ae, asg = oracle.strain_stress(spec.n, xi, eps, C11, C12, C44, sig)
+    e, s = e.reshape(9, -1), s.reshape(9, -1)
+    if "eps" in z:
+        re, rs = z["eps"], z["sigma"]
+    else:
+        idx = z["sample_idx"]
+        e, s, re, rs = e[:, idx], s[:, idx], z["eps_sample"], z["sigma_sample"]
+    assert np.max(np.abs(e - re)) <= 1e-12
+    assert np.max(np.abs(s - rs)) <= 1e-12
+    np.testing.assert_allclose(ae.ravel(), z["aveps_txt"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(asg.ravel() / C44, z["avesigma_over_mu_txt"], rtol=1e-6, atol=1e-12)
+    # the applied stress is the average stress
+    np.testing.assert_allclose(asg, sig * C44, atol=1e-12)
