@@ -147,6 +147,19 @@ pfdd_status pfdd_set_stream_priority(pfdd_ctx *ctx, int priority);
 pfdd_status pfdd_set_kernel_timing(pfdd_ctx *ctx, int enable);
 pfdd_status pfdd_kernel_stat(pfdd_ctx *ctx, int idx, const char **name, long long *launches, double *total_ms);
 
+/* Strain and stress fields of replica r's current state, in FP64 whatever the
+ * context's precision: the reference's strain (F:752-835, with the F matrix of
+ * Fmatrix, F:414-598, and the microscopic strain of avestrain, F:641-749) and
+ * stress (F:837-972), and their grid means (F:4063-4072, F:920).  sigma_app
+ * [3][3]: the uniform applied stress in units of C44 (the reference's sigma
+ * array, setstress F:3820-3918).  Outputs, each may be NULL: eps[9][N] and
+ * sigma[9][N] (component 3*i + j, the real parts of DATAEPS and DATASIGMA),
+ * aveps[9] and avesigma[9].  Needs the constants and eigenstrains of
+ * pfdd_build_B.  Uses about (ns + 6)*N complex doubles of temporary device
+ * memory for the call; the state is not changed. */
+pfdd_status pfdd_strain_stress(pfdd_ctx *ctx, int r, const double *sigma_app, double *eps, double *sigma,
+                               double *aveps, double *avesigma);
+
 /* Launch plan of the context as a JSON object: tile widths, threads and shared
  * memory of each pass, the radix plan of each axis, the steps per captured CUDA
  * graph and the autotune timings (null before the first pfdd_step, which times

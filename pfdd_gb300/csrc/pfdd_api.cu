@@ -74,6 +74,111 @@ __global__ void __launch_bounds__(256) gamma_reduce_kernel(const long long *part
     gamma[blockIdx.x] = totbad ? __longlong_as_double(0x7ff8000000000000ll) : i128_to_double(tot) * scale;
 }
 
+// ---- strain and stress fields (diagnostics) --------------------------------
+
+struct StrainParams {
+  int n1, n2, n3, ns;
+  double d1, d2, d3, mu, ll, mup;
+  double sig[kMaxNs][3][3];  // sigma_a = C : eps_a
+  double eps[kMaxNs][3][3];
+  double avepst_sym[3][3];   // (avepst + avepst^T) / 2
+  double inv_n;
+};
+
+// Symmetric strain in k-space.  The reference's F matrix (F:414-598) is
+// F_a,ij = sum_klmn C_klmn G_jk eps_a,mn f_i f_l = f_i (G t_a)_j with
+// t_a = sigma_a f, so beta_ij(k) = sum_a F_a,ij xi_a(k) = f_i w_j with
+// w = sum_a u_a xi_a, u_a = G t_a (strain, F:761-778); the kernel writes the
+// six components (f_i w_j + f_j w_i)/2, c = 00, 01, 02, 11, 12, 22.
+__global__ void strain_spec_kernel(const StrainParams *__restrict__ sp, const double2 *__restrict__ xhat,
+                                   double2 *__restrict__ E, long long N) {
+  const int ns = sp->ns;
+  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += (long long)gridDim.x * blockDim.x) {
+    const int k3 = (int)(pt % sp->n3), k2 = (int)((pt / sp->n3) % sp->n2), k1 = (int)(pt / ((long long)sp->n3 * sp->n2));
+    const double f[3] = {frec_dev(k1, sp->n1, sp->d1), frec_dev(k2, sp->n2, sp->d2), frec_dev(k3, sp->n3, sp->d3)};
+    const double f2 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    double2 w[3] = {{0, 0}, {0, 0}, {0, 0}};
+    if (f2 > 0) {
+      const double mu = sp->mu, ll = sp->ll, mup = sp->mup;
+      double z[3], den[3];
+      for (int i = 0; i < 3; ++i) { z[i] = f[i] * f[i] / f2; den[i] = mu + mup * z[i]; }
+      const double kk = 1.0 + (mu + ll) * (1 / den[0] * z[0] + 1 / den[1] * z[1] + 1 / den[2] * z[2]);
+      double G[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k)
+          G[i][k] = 1 / f2 * ((i == k ? 1.0 : 0.0) / den[k] - f[i] * f[k] / f2 / den[i] / den[k] * (mu + ll) / kk);
+      for (int a = 0; a < ns; ++a) {
+        double t[3], u[3];
+        for (int i = 0; i < 3; ++i) t[i] = sp->sig[a][i][0] * f[0] + sp->sig[a][i][1] * f[1] + sp->sig[a][i][2] * f[2];
+        for (int j = 0; j < 3; ++j) u[j] = G[j][0] * t[0] + G[j][1] * t[1] + G[j][2] * t[2];
+        const double2 x = xhat[(long long)a * N + pt];
+        for (int j = 0; j < 3; ++j) { w[j].x += u[j] * x.x; w[j].y += u[j] * x.y; }
+      }
+    }
+    int c = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j, ++c) {
+        double2 e;
+        e.x = 0.5 * (f[i] * w[j].x + f[j] * w[i].x);
+        e.y = 0.5 * (f[i] * w[j].y + f[j] * w[i].y);
+        E[(long long)c * N + pt] = e;
+      }
+  }
+}
+
+// Real-space strain and stress per point (strain F:792-812, stress F:885-921):
+// eps_ij = Re E_ij / N + sym(avepst)_ij, sigma_ij = C_ijkl (eps_kl - eps_d,kl),
+// eps_d = sum_a eps_a Re xi_a.  Outputs [3 i + j][N] (either may be null) and
+// per-block partial sums of both (18 values per block, summed on the host in
+// block order, so the means do not depend on scheduling).
+__global__ void __launch_bounds__(256) strain_real_kernel(const StrainParams *__restrict__ sp,
+                                                          const double2 *__restrict__ E,
+                                                          const double2 *__restrict__ xi, double *eps_out,
+                                                          double *sig_out, double *partial, long long N) {
+  __shared__ double red[18][256];
+  double acc[18];
+  for (int q = 0; q < 18; ++q) acc[q] = 0.0;
+  const int ns = sp->ns;
+  const double mu = sp->mu, ll = sp->ll, mup = sp->mup;
+  for (long long pt = (long long)blockIdx.x * blockDim.x + threadIdx.x; pt < N; pt += (long long)gridDim.x * blockDim.x) {
+    double e[3][3], ed[3][3];
+    int c = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j, ++c) {
+        e[i][j] = E[(long long)c * N + pt].x * sp->inv_n + sp->avepst_sym[i][j];
+        e[j][i] = e[i][j];
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) ed[i][j] = 0.0;
+    for (int a = 0; a < ns; ++a) {
+      const double x = xi[(long long)a * N + pt].x;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) ed[i][j] += sp->eps[a][i][j] * x;
+    }
+    double d[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) d[i][j] = e[i][j] - ed[i][j];
+    const double tr = d[0][0] + d[1][1] + d[2][2];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        // C_ijkl d_kl of the cubic/isotropic C (F:869-877)
+        const double s = mu * (d[i][j] + d[j][i]) + (i == j ? ll * tr + mup * d[i][i] : 0.0);
+        if (eps_out) eps_out[(long long)(3 * i + j) * N + pt] = e[i][j];
+        if (sig_out) sig_out[(long long)(3 * i + j) * N + pt] = s;
+        acc[3 * i + j] += e[i][j];
+        acc[9 + 3 * i + j] += s;
+      }
+  }
+  for (int q = 0; q < 18; ++q) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 18; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 18) partial[(long long)blockIdx.x * 18 + threadIdx.x] = red[threadIdx.x][0];
+}
+
 // B(k) of Bmatrix (F:328-412) in closed form:
 //   B_ab = (E_ab - t_a^T G t_b) / mu,  t_a = sigma_a f,
 //   G_ki = (1/f^2) [delta_ik / (mu + mu' z_k)
@@ -246,6 +351,10 @@ struct pfdd_ctx {
   unsigned gen = 0, graph_gen = ~0u;
   bool primed = false, use_graphs = true;
   // launch plan: tile widths timed on the first step (autotune), as JSON
+  // elastic constants, eigenstrains and spacings of pfdd_build_B (strain/stress)
+  bool hasElastic = false;
+  double Cel[3] = {0, 0, 0}, dsp[3] = {1, 1, 1};
+  std::vector<double> epsv;
   bool tuned = false, tune = true;
   int zparts_cap = 0;  // z-pass blocks per field the partial buffer holds
   std::string plan;
@@ -515,6 +624,10 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
         for (int j = 0; j < 3; ++j) s += eps[(a * 3 + i) * 3 + j] * hp.sig[b][i][j];
       hp.E[a][b] = s;
     }
+  c->Cel[0] = C11; c->Cel[1] = C12; c->Cel[2] = C44;
+  c->dsp[0] = d1; c->dsp[1] = d2; c->dsp[2] = d3;
+  c->epsv.assign(eps, eps + 9 * c->ns);
+  c->hasElastic = true;
   if (c->prec == PFDD_FFT_FP32_BFLY) {  // the x-pass evaluates the same closed form in FP32
     BFlyParams &bf = c->bf;
     bf.n2 = c->n[1]; bf.n3 = c->n[2]; bf.lgN3 = ilog2(c->n[2]);
@@ -1124,4 +1237,118 @@ extern "C" pfdd_status pfdd_fft_forward(pfdd_fft_plan *p, void *data, int batch,
 }
 extern "C" pfdd_status pfdd_fft_backward(pfdd_fft_plan *p, void *data, int batch, int on_device) {
   return fft_call(p, data, batch, on_device, +1);
+}
+
+// ---- strain and stress fields of a state (strain F:752-835, stress F:837-972)
+
+extern "C" pfdd_status pfdd_strain_stress(pfdd_ctx *c, int r, const double *sigma_app, double *eps, double *sigma,
+                                          double *aveps, double *avesigma) {
+  if (!c || !sigma_app || r < 0 || r >= c->nrep) return fail(c, PFDD_EINVAL, "pfdd_strain_stress: bad argument");
+  if (!c->hasElastic)
+    return fail(c, PFDD_ENOTREADY, "pfdd_strain_stress: needs the elastic constants and eigenstrains of pfdd_build_B");
+  if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_strain_stress: state not set");
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaStreamSynchronize(c->st));  // the state is current
+  const int ns = c->ns;
+  const long long N = c->N;
+  const double C11 = c->Cel[0], C12 = c->Cel[1], C44 = c->Cel[2];
+  StrainParams hp;
+  std::memset(&hp, 0, sizeof hp);
+  hp.n1 = c->n[0]; hp.n2 = c->n[1]; hp.n3 = c->n[2]; hp.ns = ns;
+  hp.d1 = c->dsp[0]; hp.d2 = c->dsp[1]; hp.d3 = c->dsp[2];
+  hp.mu = C44; hp.ll = C12; hp.mup = C11 - C12 - 2 * C44;
+  hp.inv_n = 1.0 / (double)N;
+  double Cc[3][3][3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k)
+        for (int m = 0; m < 3; ++m)
+          Cc[i][j][k][m] = hp.mu * ((i == k) * (j == m) + (i == m) * (j == k)) + hp.ll * (i == j) * (k == m) +
+                           hp.mup * ((i == j) && (j == k) && (k == m));
+  for (int a = 0; a < ns; ++a)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double s = 0;
+        for (int m = 0; m < 3; ++m)
+          for (int n = 0; n < 3; ++n) s += Cc[i][j][m][n] * c->epsv[(a * 3 + m) * 3 + n];
+        hp.sig[a][i][j] = s;
+        hp.eps[a][i][j] = c->epsv[(a * 3 + i) * 3 + j];
+      }
+  // FP64 work: a natural-layout FFT plan whose buffer holds the state's transform
+  pfdd_fft_plan *p = nullptr;
+  pfdd_status st = pfdd_fft_plan_create(&p, c->n[0], c->n[1], c->n[2], PFDD_FP64, std::max(ns, 6), c->dev);
+  if (st != PFDD_OK) return fail(c, st, "pfdd_strain_stress: work buffers (%s)", pfdd_status_string(st));
+  const int blocks = (int)std::min<long long>(1216, (N + 255) / 256);
+  double2 *E = nullptr;
+  double *d_eps = nullptr, *d_sig = nullptr, *part = nullptr;
+  StrainParams *dp = nullptr;
+  std::vector<double2> dc(ns);
+  std::vector<double> hpart((size_t)blocks * 18);
+  double2 *W = reinterpret_cast<double2 *>(p->buf);
+  cudaError_t e = cudaMalloc(&E, 6 * N * sizeof(double2));
+  if (e == cudaSuccess && eps) e = cudaMalloc(&d_eps, 9 * N * sizeof(double));
+  if (e == cudaSuccess && sigma) e = cudaMalloc(&d_sig, 9 * N * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&part, hpart.size() * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof hp);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(W, c->xi + (size_t)r * ns * N, (size_t)ns * N * sizeof(double2), cudaMemcpyDeviceToDevice, p->st);
+  if (e == cudaSuccess) e = fft_exec(p, W, ns, -1);
+  // the k = 0 coefficients are the field sums: <Re xi_a> for avepsd (avestrain, F:670-688)
+  for (int a = 0; e == cudaSuccess && a < ns; ++a)
+    e = cudaMemcpyAsync(&dc[a], W + (size_t)a * N, sizeof(double2), cudaMemcpyDeviceToHost, p->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  if (e == cudaSuccess) {
+    // avepst = S : sigma_app mu + avepsd (F:726-741), S of F:661-664 with S11, S12, S44 of F:4261-4263
+    const double S11 = 1. / 3. * (1 / (C11 + 2 * C12) + 2 / (C11 - C12));
+    const double S12 = 1. / 3. * (1 / (C11 + 2 * C12) - 1 / (C11 - C12));
+    const double S44 = 1 / C44;
+    double avepst[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double s = 0.;
+        for (int k = 0; k < 3; ++k)
+          for (int l = 0; l < 3; ++l) {
+            const double dij = i == j, dkl = k == l, d4 = (i == j) && (j == k) && (k == l);
+            const double Sijkl = (S11 + 2 * S12) / 3.0 * dij * dkl + S44 / 4.0 * ((i == k) * (j == l) + (i == l) * (j == k)) -
+                                 S44 / 2.0 * d4 + (S11 - S12) * (d4 - dij * dkl / 3.0);
+            s += Sijkl * sigma_app[3 * k + l] * C44;
+          }
+        double ad = 0.;
+        for (int a = 0; a < ns; ++a) ad += hp.eps[a][i][j] * (dc[a].x / (double)N);
+        avepst[i][j] = s + ad;
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) hp.avepst_sym[i][j] = 0.5 * (avepst[i][j] + avepst[j][i]);
+    e = cudaMemcpyAsync(dp, &hp, sizeof hp, cudaMemcpyHostToDevice, p->st);
+  }
+  if (e == cudaSuccess) {
+    strain_spec_kernel<<<1216, 256, 0, p->st>>>(dp, W, E, N);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = fft_exec(p, E, 6, +1);
+  if (e == cudaSuccess) {
+    strain_real_kernel<<<blocks, 256, 0, p->st>>>(dp, E, c->xi + (size_t)r * ns * N, d_eps, d_sig, part, N);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && eps) e = cudaMemcpyAsync(eps, d_eps, 9 * N * sizeof(double), cudaMemcpyDeviceToHost, p->st);
+  if (e == cudaSuccess && sigma) e = cudaMemcpyAsync(sigma, d_sig, 9 * N * sizeof(double), cudaMemcpyDeviceToHost, p->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hpart.data(), part, hpart.size() * sizeof(double), cudaMemcpyDeviceToHost, p->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  if (e == cudaSuccess) {
+    for (int q = 0; q < 9; ++q) {
+      double se = 0., ss = 0.;
+      for (int b = 0; b < blocks; ++b) {
+        se += hpart[(size_t)b * 18 + q];
+        ss += hpart[(size_t)b * 18 + 9 + q];
+      }
+      if (aveps) aveps[q] = se / (double)N;
+      if (avesigma) avesigma[q] = ss / (double)N;
+    }
+  }
+  for (void *q : {(void *)E, (void *)d_eps, (void *)d_sig, (void *)part, (void *)dp})
+    if (q) cudaFree(q);
+  pfdd_fft_plan_destroy(p);
+  CK(c, e);
+  return PFDD_OK;
 }

@@ -8,10 +8,15 @@
  * F:1540-1637), builds B(k) on the GPU (Bmatrix F:328-412), runs K TDGL steps
  * with a linear stress ramp (plasticevolv F:3470-3501, loop F:4574-4691),
  * and writes phasefield.dat (F:4672), gamma_full.dat (full precision) and
- * xi.dat (F:4777-4788) in the working directory.
+ * xi.dat (F:4777-4788) in the working directory.  With --strain it also
+ * writes strain.txt (F:818-831) and stress.txt (F:927-944) of the state it
+ * starts from, and stress-strain.dat (F:4063-4072, 4694-4698): the grid means
+ * of strain and stress (over C44) of the starting state and of the final
+ * state, then the final gamma_a and gamma.
  *
  * usage: pfdd_run N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C]
  *                 [--mu MU] [--lambda LAM] [--bdiv BD] [--fp32] [--device D]
+ *                 [--strain]
  *
  * NSF (default NS) is the slip-system count of the files; systems NS..NSF-1
  * and the 9 virtual-strain fields must be zero and pinned (they contribute
@@ -37,15 +42,44 @@ static int die(const char *msg, pfdd_ctx *c, int st) {
   return 1;
 }
 
+/* strain.txt (F:818-831) and stress.txt (F:927-944, rows with j == 0); the
+ * first six stress columns are the applied stress field (SIGMAV, which holds
+ * it when no virtual strain evolves), the next six the stress field. */
+static int write_fields(int n1, int n2, int n3, const double *e, const double *sg, const double sig[3][3]) {
+  const long N = (long)n1 * n2 * n3;
+  FILE *f3 = fopen("strain.txt", "w"), *f5 = fopen("stress.txt", "w");
+  if (!f3 || !f5) return 1;
+  fprintf(f3, "x,y,z,eps11,eps13,eps21,eps22,eps23,eps31,eps32,eps33\n");
+  fprintf(f5, "x,y,z,sigma11,sigma12,sigma13,sigma22,sigma23,sigma33,datasigma11,datasigma12,datasigma13,datasigma22,"
+              "datasigma23,datasigma33 \n");
+  for (int i = 0; i < n1; ++i)
+    for (int j = 0; j < n2; ++j)
+      for (int k = 0; k < n3; ++k) {
+        const long pt = ((long)i * n2 + j) * n3 + k;
+        fprintf(f3, "%d,%d,%d", i, j, k);
+        for (int q = 0; q < 9; ++q) fprintf(f3, ",%lf", e[(long)q * N + pt]);
+        fprintf(f3, " \n");
+        if (j == 0) {
+          fprintf(f5, "%d,%d,%d,%lf,%lf,%lf,%lf,%lf,%lf", i, j, k, sig[0][0], sig[0][1], sig[0][2], sig[1][1],
+                  sig[1][2], sig[2][2]);
+          const int comp[6] = {0, 1, 2, 4, 5, 8};
+          for (int q = 0; q < 6; ++q) fprintf(f5, ",%lf", sg[(long)comp[q] * N + pt]);
+          fprintf(f5, "\n");
+        }
+      }
+  fclose(f3); fclose(f5);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 7) {
     fprintf(stderr, "usage: %s N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C] [--mu MU] [--lambda LAM] "
-                    "[--bdiv BD] [--fp32] [--device D]\n", argv[0]);
+                    "[--bdiv BD] [--fp32] [--device D] [--strain]\n", argv[0]);
     return 2;
   }
   int n1 = atoi(argv[1]), n2 = atoi(argv[2]), n3 = atoi(argv[3]), ns = atoi(argv[4]), K = atoi(argv[5]);
   double sigma_max = atof(argv[6]);
-  int nsf = ns, prec = PFDD_FP64, dev = 0;
+  int nsf = ns, prec = PFDD_FP64, dev = 0, strain = 0;
   double asf = 0.1, cd2 = 0.01, mu = 1.0, lam = 1.5, bdiv = sqrt(2.0);
   for (int i = 7; i < argc; ++i) {
     if (!strcmp(argv[i], "--nsfile") && i + 1 < argc) nsf = atoi(argv[++i]);
@@ -56,6 +90,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[i], "--bdiv") && i + 1 < argc) bdiv = atof(argv[++i]);
     else if (!strcmp(argv[i], "--fp32")) prec = PFDD_FFT_FP32;
     else if (!strcmp(argv[i], "--device") && i + 1 < argc) dev = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--strain")) strain = 1;
     else { fprintf(stderr, "unknown option %s\n", argv[i]); return 2; }
   }
   if (ns < 1 || ns > 12 || nsf < ns || K < 1) { fprintf(stderr, "bad NS/K\n"); return 2; }
@@ -98,6 +133,14 @@ int main(int argc, char **argv) {
   if ((st = pfdd_set_params(c, cdv, asfv, dslip, 1.0)) != PFDD_OK) return die("set_params", c, st);
   if ((st = pfdd_set_state(c, xi, bc)) != PFDD_OK) return die("set_state", c, st);
   double *gamma = malloc(sizeof(double) * K), *gamma_a = malloc(sizeof(double) * (size_t)K * ns);
+  double ave0[2][9], ave1[2][9];
+  if (strain) {  /* strain and stress of the starting state (outer step before the inner loop) */
+    double *e = malloc(sizeof(double) * 9 * (size_t)N), *sg = malloc(sizeof(double) * 9 * (size_t)N);
+    if (!e || !sg) { fprintf(stderr, "out of host memory\n"); return 1; }
+    if ((st = pfdd_strain_stress(c, 0, &sig[0][0], e, sg, ave0[0], ave0[1])) != PFDD_OK) return die("strain", c, st);
+    if (write_fields(n1, n2, n3, e, sg, (const double(*)[3])sig)) { fprintf(stderr, "cannot write strain.txt\n"); return 1; }
+    free(e); free(sg);
+  }
   double t1 = wtime();
   if ((st = pfdd_step(c, K, tau, gamma, gamma_a)) != PFDD_OK) return die("step", c, st);
   double t2 = wtime();
@@ -113,6 +156,16 @@ int main(int argc, char **argv) {
     fprintf(gf, "\n");
   }
   fclose(pf); fclose(gf);
+  if (strain) {  /* stress-strain.dat: means (stress over C44) of the start and final states, gamma */
+    if ((st = pfdd_strain_stress(c, 0, &sig[0][0], NULL, NULL, ave1[0], ave1[1])) != PFDD_OK) return die("strain", c, st);
+    FILE *f2 = fopen("stress-strain.dat", "w");
+    if (!f2) { fprintf(stderr, "cannot write stress-strain.dat\n"); return 1; }
+    for (int q = 0; q < 9; ++q) fprintf(f2, "%e %e ", ave0[0][q], ave0[1][q] / C44);
+    for (int q = 0; q < 9; ++q) fprintf(f2, "%e %e ", ave1[0][q], ave1[1][q] / C44);
+    for (int a = 0; a < nsf; ++a) fprintf(f2, "\t%e", a < ns ? gamma_a[(size_t)(K - 1) * ns + a] : 0.0);
+    fprintf(f2, " %e \n", gamma[K - 1]);
+    fclose(f2);
+  }
   FILE *fo = fopen("xi.dat", "r+b");
   if (!fo || fwrite(xi, sizeof(double), cnt, fo) != cnt) { fprintf(stderr, "cannot write xi.dat\n"); return 1; }
   fclose(fo);

@@ -32,6 +32,7 @@ EXPORTS = [
     "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
     "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
     "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority", "pfdd_get_plan",
+    "pfdd_strain_stress",
 ]
 
 _lib = None
@@ -76,6 +77,7 @@ def load():
     L.pfdd_get_stream.restype = vp
     L.pfdd_set_stream_priority.argtypes = [vp, i]
     L.pfdd_get_plan.argtypes = [vp, C.c_char_p, sz]
+    L.pfdd_strain_stress.argtypes = [vp, i, dp, dp, dp, dp, dp]
     L.pfdd_set_kernel_timing.argtypes = [vp, i]
     L.pfdd_kernel_stat.argtypes = [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     L.pfdd_required_bytes.argtypes = [i, i, i, i, i, i]
@@ -260,6 +262,18 @@ class Solver:
 
     def kernel_timing(self, on: bool):
         self._check(self.L.pfdd_set_kernel_timing(self.h, int(bool(on))), "pfdd_set_kernel_timing")
+
+    def strain_stress(self, sigma_app: np.ndarray, r: int = 0, fields: bool = True):
+        """Strain and stress of replica r: (eps [3,3,N], sigma [3,3,N], aveps [3,3],
+        avesigma [3,3]); the fields are None with fields=False."""
+        sa = _f64(sigma_app).reshape(9)
+        e = np.zeros((9, self.N)) if fields else None
+        s = np.zeros((9, self.N)) if fields else None
+        ae = np.zeros(9); asg = np.zeros(9)
+        self._check(self.L.pfdd_strain_stress(self.h, r, _dp(sa), _dp(e), _dp(s), _dp(ae), _dp(asg)),
+                    "pfdd_strain_stress")
+        rs = (lambda a: None if a is None else a.reshape(3, 3, self.N))
+        return rs(e), rs(s), ae.reshape(3, 3), asg.reshape(3, 3)
 
     def plan(self) -> dict:
         """Launch plan (tile widths, threads, shared memory, radix plans, autotune timings)."""
