@@ -382,6 +382,28 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     }
 
 
+def time_strain(native, workloads, spec, dev, reps=3):
+    """pfdd_strain_stress on the solve's initial state (FP64 fields, reference
+    strain/stress outputs): wall time per call with the 9+9 fields copied to the
+    host, and with the means only."""
+    s = native.solver_for(spec, "fp32", device=dev)
+    s.set_state(*workloads.initial_state(spec))
+    sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
+    s.strain_stress(sig, fields=False)  # warm
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        s.strain_stress(sig, fields=True)
+    t1 = time.perf_counter()
+    for _ in range(reps):
+        _, _, ae, asg = s.strain_stress(sig, fields=False)
+    t2 = time.perf_counter()
+    s.close()
+    return {"ms_with_fields": round(1e3 * (t1 - t0) / reps, 2), "ms_means_only": round(1e3 * (t2 - t1) / reps, 2),
+            "aveps": [round(float(v), 9) for v in ae.ravel()],
+            "avesigma": [round(float(v), 9) for v in asg.ravel()],
+            "what": "strain and stress fields (FP64) of the 128^3 x 12 initial state incl. work-buffer setup"}
+
+
 def run_batched(native, workloads, dev, K, K64, W=3, count=16):
     """Batched stress sweep: `count` replicas of the 128^3 x 12 solve in one
     context sharing B(k) (FP32-FFT form), aggregate steps/s; each replica's
@@ -495,6 +517,9 @@ def run_ours(a):
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline and r64["B"] is not None:
         cpu = cpu_baseline_port(spec, r64["B"])
+    strain = None
+    if dist.world == 1:
+        strain = time_strain(native, workloads, spec, dev)
     batched = None
     if dist.world == 1 and a.batched_steps > 0:
         batched = run_batched(native, workloads, dev, a.batched_steps, max(5, a.batched_steps // 8))
@@ -528,7 +553,7 @@ def run_ours(a):
                   "strain_rel_err_fp32_vs_fp64": strain_err, "strain_err_steps": kk},
         "kernels": kern, "plan": r32["plan"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(r32["launches"]), "launches_per_step": round(launches_per_step, 2),
-        "clocks": r32["clocks"], "batched": batched, "serving": serving,
+        "clocks": r32["clocks"], "strain_stress": strain, "batched": batched, "serving": serving,
     }
     if dist.rank == 0:
         print(json.dumps(out), flush=True)

@@ -487,6 +487,10 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   CK(c, cudaSetDevice(device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision), /*xfast=*/true);
+  if (!c->g.valid)
+    return fail(c, PFDD_EINVAL,
+                "pfdd_create: one x-line tile of %d systems x N1=%d with its B(k) does not fit in shared memory in "
+                "this precision", ns, n1);
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
   CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
   CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));

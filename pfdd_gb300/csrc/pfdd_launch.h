@@ -38,7 +38,12 @@ inline int ilog2(long long v) {
   return l;
 }
 
+// dynamic shared memory a kernel may opt into (227 KB per block on GB300,
+// less the kernels' few hundred bytes of static shared memory)
+constexpr size_t kMaxDynSmem = 226 * 1024;
+
 struct Geometry {
+  bool valid = true;  // false: the fused x-pass tile of this grid does not fit
   // spectral layout of a context's S: x fastest ([y][z][x] per field); the
   // FFT-boundary plans keep the natural [x][y][z]
   bool xfast = false;
@@ -79,7 +84,7 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   // twiddles + padded S lines (16-byte aligned) + FP64 xi tile
   g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
   g.lgL3 = ilog2(L3);
-  return g.zSmem <= 200 * 1024;
+  return g.zSmem <= kMaxDynSmem;
 }
 
 // Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.
@@ -92,7 +97,7 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
   g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
   g.tiles[ax] = inner / TI;
   g.smem[ax] = ((size_t)L + (size_t)L * g.pitch[ax]) * vsize;
-  return g.smem[ax] <= 200 * 1024;
+  return g.smem[ax] <= kMaxDynSmem;
 }
 
 // Fused x-pass with tiles of T = 2^lgT inner indices (all N1 x, all ns fields,
@@ -102,7 +107,7 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
   if ((1LL << lgT) > innerx) return false;
   const int pitch = line_pitch(n1);
   const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize);
-  if (smem > 200 * 1024) return false;
+  if (smem > kMaxDynSmem) return false;
   const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
   const int unit = std::max(32, team);
   const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
@@ -143,7 +148,7 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
     while (lgT > 0 && ((1LL << lgT) > (long long)n2 * n3 ||
                        x_fused_smem(ns, n1, lgT, line_pitch(n1), vsize, bsize) > 110 * 1024))
       --lgT;
-    set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
+    g.valid = set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
   }
   return g;
 }

@@ -1,0 +1,88 @@
+"""Launch geometry checked on the host before any GPU run: for every grid the
+workloads and tests use (and every autotune candidate), the shared memory, thread
+counts and tilings that the kernels assume hold.  The geometry code is the
+library's own header, compiled here with nvcc as host code (no GPU needed)."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+HARNESS = r"""
+#include <cstdio>
+#include "pfdd_launch.h"
+using namespace pfdd;
+static int bad = 0, checked = 0;
+#define CHECK(c, what) do { if (!(c)) { ++bad; std::printf("FAIL %s n=%dx%dx%d ns=%d v=%zu b=%zu\n", what, n1, n2, n3, ns, vs, bs); } } while (0)
+static void z_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
+  const int team = n3 / (n3 < 8 ? n3 : 8);
+  CHECK((g.zTL & (g.zTL - 1)) == 0 && g.zTL <= n1 && n1 % g.zTL == 0, "z lines");
+  CHECK(g.zThreads == g.zTL * team && g.zThreads <= kThreads, "z threads");
+  CHECK(g.zSmem <= kMaxDynSmem && g.zPitch >= n3 + 1, "z smem/pitch");
+  CHECK((long long)g.zNparts * g.zTL == (long long)n1 * n2, "z parts");
+}
+static void y_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
+  const long long inner = (long long)n3 * n1;
+  const int team = n2 / (n2 < 8 ? n2 : 8);
+  const int TI = 1 << g.lgTI[0];
+  CHECK(TI <= inner && inner % TI == 0 && g.tiles[0] * TI == inner, "y tiles");
+  CHECK(g.threads[0] == TI * team && g.threads[0] <= kThreads && g.smem[0] <= kMaxDynSmem, "y threads/smem");
+}
+static void x_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
+  const int team = n1 / (n1 < 8 ? n1 : 8);
+  const int cap = (vs == 16 || bs == 0) ? 256 : 384;
+  CHECK(g.xTiles << g.xLgT == (long long)n2 * n3, "x tiles");
+  CHECK(g.xThreads >= team && g.xThreads % team == 0 && g.xThreads <= cap, "x threads");
+  CHECK(g.xSmem == x_fused_smem(ns, n1, g.xLgT, g.xPitch, vs, bs) && g.xSmem <= kMaxDynSmem, "x smem");
+}
+int main() {
+  const int sizes[][3] = {{8, 8, 8}, {16, 16, 16}, {32, 32, 32}, {64, 64, 64}, {128, 128, 128}, {256, 256, 256},
+                          {8, 16, 32}, {32, 2, 32}, {16, 8, 32}, {32, 16, 64}, {8, 16, 16}, {16, 8, 16}, {16, 16, 32},
+                          {512, 8, 8}, {8, 8, 512}, {4, 4, 4}, {2, 64, 2}};
+  const size_t vb[3][2] = {{16, 8}, {8, 4}, {8, 0}};
+  for (auto &sz : sizes)
+    for (int ns : {1, 3, 12})
+      for (auto &p : vb) {
+        const int n1 = sz[0], n2 = sz[1], n3 = sz[2];
+        const size_t vs = p[0], bs = p[1];
+        if (bs == 0 && (n1 < 32 || n1 > 256)) continue;  // the on-the-fly form's range
+        Geometry g = make_geometry(n1, n2, n3, ns, vs, bs, true);
+        const bool expect_fit = x_fused_smem(ns, n1, 0, line_pitch(n1), vs, bs) <= kMaxDynSmem;
+        CHECK(g.valid == expect_fit, "validity");
+        if (!g.valid) continue;
+        ++checked;
+        z_ok(g, n1, n2, n3, ns, vs, bs); y_ok(g, n1, n2, n3, ns, vs, bs); x_ok(g, n1, n2, n3, ns, vs, bs);
+        const int cap = (int)std::min<long long>((long long)n1 * n2, (long long)g.zNparts * 4);
+        for (int lg = 0; lg <= 5; ++lg) {
+          Geometry h = g;
+          if (set_z_geometry(h, n1, n2, n3, vs, 1 << lg) && h.zNparts <= cap) z_ok(h, n1, n2, n3, ns, vs, bs);
+          h = g;
+          if (set_x_geometry(h, n1, n2, n3, ns, vs, bs, lg)) x_ok(h, n1, n2, n3, ns, vs, bs);
+        }
+        for (int lg = 0; lg <= 7; ++lg) {
+          Geometry h = g;
+          if (set_strided_geometry(h, 0, n2, (long long)n3 * n1, lg, vs)) y_ok(h, n1, n2, n3, ns, vs, bs);
+        }
+      }
+  std::printf("%d %d\n", checked, bad);
+  return 0;
+}
+"""
+
+
+def test_launch_geometry_invariants(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        pytest.skip("nvcc not available")
+    src = tmp_path / "geom.cu"
+    src.write_text(HARNESS)
+    exe = tmp_path / "geom"
+    subprocess.run([nvcc, "-std=c++17", "-O1", "-I", str(ROOT / "pfdd_gb300" / "csrc"), "-I", str(ROOT / "include"),
+                    str(src), "-o", str(exe)], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    *fails, last = out.strip().splitlines()
+    checked, bad = map(int, last.split())
+    assert bad == 0, fails[:20]
+    assert checked > 100
