@@ -907,11 +907,19 @@ static pfdd_status autotune(pfdd_ctx *c) {
     const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
     Geometry best = c->g;
     double bt = 1e30;
+    // the timings take one replica (the kernels skip idle ones), so tuning a
+    // batched context costs what tuning one solve does
+    if (c->nrep > 1) {
+      std::vector<uint8_t> one(c->nrep, 0);
+      one[0] = 1;
+      CK(c, cudaMemcpyAsync(c->active, one.data(), c->nrep, cudaMemcpyHostToDevice, c->st));
+      CK(c, cudaStreamSynchronize(c->st));
+    }
     // z-pass lines per block (the gamma partials are exact integer sums, so
     // the split of points into blocks changes no result); a typical state
     // (0.5) and zero stresses so the update takes its usual path
     fill_u64_kernel<<<1216, kThreads, 0, c->st>>>(reinterpret_cast<unsigned long long *>(c->xi),
-                                                  (long long)c->nrep * c->ns * c->N * 2, 0x3fe0000000000000ull);
+                                                  (long long)c->ns * c->N * 2, 0x3fe0000000000000ull);
     cudaMemsetAsync(c->tau, 0, (size_t)c->nrep * c->ns * sizeof(double), c->st);
     for (int lgTL = 0; lgTL <= 5; ++lgTL) {
       Geometry g = c->g;
@@ -957,6 +965,10 @@ static pfdd_status autotune(pfdd_ctx *c) {
     cudaEventDestroy(e1);
     c->launches = l0;
     c->tm.on = timing;
+    if (c->nrep > 1) {  // every replica active again
+      CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), c->nrep, cudaMemcpyHostToDevice, c->st));
+      CK(c, cudaStreamSynchronize(c->st));
+    }
     c->specValid = false;
     c->gen++;  // captured launch shapes change
     tuning = "{\"z_pass_us_by_lines\": {" + zs + "}, \"x_pass_us_by_tile\": {" + xs + "}, \"y_pass_us_by_tile\": {" +
