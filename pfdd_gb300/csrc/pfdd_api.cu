@@ -15,6 +15,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -852,6 +854,21 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   return b;
 }
 
+// Tuned plans by grid shape (N1, N2, N3, ns, precision, device): a process
+// times each shape once; later contexts of the shape (serving classes, batch
+// re-creation) reuse the plan instead of timing under whatever else is running.
+struct TunedPlan {
+  int zTL, xLgT, yLgTI;
+  std::string timings;
+};
+static std::mutex g_plan_mu;
+static std::map<std::string, TunedPlan> g_plans;
+
+static std::string plan_key(const pfdd_ctx *c) {
+  return std::to_string(c->n[0]) + "x" + std::to_string(c->n[1]) + "x" + std::to_string(c->n[2]) + "/" +
+         std::to_string(c->ns) + "/" + std::to_string(c->prec) + "/" + std::to_string(c->dev);
+}
+
 // Times every tile width of the fused x-pass and of the y-pass that fits, on
 // the context's own buffers (3 launches each after one warm-up), and keeps the
 // fastest.  Tile widths change no result: every line and every point is
@@ -886,6 +903,24 @@ static pfdd_status autotune(pfdd_ctx *c) {
     return PFDD_OK;
   }
   if (c->tune) {
+    const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
+    const std::string key = plan_key(c);
+    {
+      std::lock_guard<std::mutex> lk(g_plan_mu);
+      auto it = g_plans.find(key);
+      if (it != g_plans.end()) {
+        Geometry g = c->g;
+        if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
+            set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT) &&
+            (c->n[1] == 1 ||
+             set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs))) {
+          c->g = g;
+          c->gen++;
+          c->plan = plan_json(c, "{\"cached\": true, \"timings\": " + it->second.timings + "}");
+          return PFDD_OK;
+        }
+      }
+    }
     const bool timing = c->tm.on;
     c->tm.on = false;
     const long long l0 = c->launches;
@@ -904,7 +939,6 @@ static pfdd_status autotune(pfdd_ctx *c) {
       return 1e3 * ms / 3.0;
     };
     std::string xs, ys, zs;
-    const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
     Geometry best = c->g;
     double bt = 1e30;
     // the timings take one replica (the kernels skip idle ones), so tuning a
@@ -973,6 +1007,10 @@ static pfdd_status autotune(pfdd_ctx *c) {
     c->gen++;  // captured launch shapes change
     tuning = "{\"z_pass_us_by_lines\": {" + zs + "}, \"x_pass_us_by_tile\": {" + xs + "}, \"y_pass_us_by_tile\": {" +
              ys + "}}";
+    {
+      std::lock_guard<std::mutex> lk(g_plan_mu);
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], tuning};
+    }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }
   c->plan = plan_json(c, tuning);

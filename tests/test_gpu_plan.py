@@ -38,7 +38,10 @@ def test_tuned_plan_gives_same_bits(native_lib, precision):
     np.testing.assert_array_equal(g1, g0)
     np.testing.assert_array_equal(x1, x0)
     assert p0["autotune"] is None
-    tried = p1["autotune"]["x_pass_us_by_tile"]
+    tune = p1["autotune"]
+    if tune.get("cached"):  # an earlier context of this shape was tuned in this process
+        tune = tune["timings"]
+    tried = tune["x_pass_us_by_tile"]
     assert len(tried) >= 1 and all(v > 0 for v in tried.values())
     assert str(p1["x_pass"]["tile_columns"]) in tried
     assert p1["radix_plan"] == ["8x4", "8x2", "8x8"]
@@ -57,3 +60,13 @@ def test_pinned_plan(native_lib):
     assert (p1["z_pass"]["lines"], p1["x_pass"]["tile_columns"], p1["y_pass"]["tile_columns"]) == (8, 2, 8)
     np.testing.assert_array_equal(g1, g0)
     np.testing.assert_array_equal(x1, x0)
+
+
+def test_plan_is_tuned_once_per_shape(native_lib):
+    spec = workloads.SolveSpec(n=(16, 32, 16), ns=3, steps=3, sigma_max=0.02, noise_seed=23)
+    g1, x1, p1 = run(spec, "fp32", True)
+    g2, x2, p2 = run(spec, "fp32", True)
+    assert p2["autotune"]["cached"] is True
+    assert (p2["z_pass"], p2["x_pass"], p2["y_pass"]) == (p1["z_pass"], p1["x_pass"], p1["y_pass"])
+    np.testing.assert_array_equal(g1, g2)
+    np.testing.assert_array_equal(x1, x2)
