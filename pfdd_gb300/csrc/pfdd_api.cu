@@ -859,6 +859,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
   int zTL, xLgT, yLgTI;
+  bool xWide;
   std::string timings;
 };
 static std::mutex g_plan_mu;
@@ -911,7 +912,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
       if (it != g_plans.end()) {
         Geometry g = c->g;
         if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
-            set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT) &&
+            set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide) &&
             (c->n[1] == 1 ||
              set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs))) {
           c->g = g;
@@ -970,14 +971,16 @@ static pfdd_status autotune(pfdd_ctx *c) {
     }
     c->g = best;
     bt = 1e30;
-    for (int lgT = 0; lgT <= 6; ++lgT) {
+    for (int cand = 0; cand <= 13; ++cand) {
+      const int lgT = cand >> 1;
+      const bool wide = cand & 1;
       Geometry g = c->g;
-      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT)) continue;
+      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide)) continue;
       c->g = g;
       const double us = time_us([&] { return launch_x_fused<T>(c); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
-      snprintf(b, sizeof b, "%s\"%d\": %.1f", xs.empty() ? "" : ", ", 1 << lgT, us);
+      snprintf(b, sizeof b, "%s\"%d%s\": %.1f", xs.empty() ? "" : ", ", 1 << lgT, wide ? "w" : "", us);
       xs += b;
     }
     c->g = best;
@@ -1009,7 +1012,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
              ys + "}}";
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], tuning};
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.xWide, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }

@@ -56,6 +56,7 @@ struct Geometry {
   size_t smem[2] = {0, 0};
   // fused x-pass
   int xLgT = 0, xPitch = 1, xThreads = 256;
+  bool xWide = false;
   long long xTiles = 1;
   size_t xSmem = 0;
 };
@@ -102,7 +103,12 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
 
 // Fused x-pass with tiles of T = 2^lgT inner indices (all N1 x, all ns fields,
 // the tile's B(k)).  False when the tile does not fit.
-inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT) {
+// wide: enough threads that the lines of a tile fill whole shared-memory
+// phases (16 lanes of 8 bytes, 8 of 16 bytes), i.e. every phase of an FFT
+// stage touches as many different lines as it has lanes (no bank conflicts),
+// at the price of idle threads when the tile has fewer lines.
+inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT,
+                           bool wide = false) {
   const long long innerx = (long long)n2 * n3;
   if ((1LL << lgT) > innerx) return false;
   const int pitch = line_pitch(n1);
@@ -112,13 +118,17 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
   const int unit = std::max(32, team);
   const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
   if (unit > cap) return false;
-  int thr = std::min(cap, std::max(npt, lines * team));
+  const int phase = (int)(128 / vsize);
+  const int lines_eff = wide ? (lines + phase - 1) / phase * phase : lines;
+  if (wide && (lines_eff == lines || lines_eff * team > cap)) return false;  // nothing to widen / too wide
+  int thr = std::min(cap, std::max(npt, lines_eff * team));
   thr = (thr + unit - 1) / unit * unit;
   g.xPitch = pitch;
   g.xLgT = lgT;
   g.xTiles = innerx >> lgT;
   g.xSmem = smem;
   g.xThreads = std::min(thr, cap / unit * unit);
+  g.xWide = wide;
   return true;
 }
 

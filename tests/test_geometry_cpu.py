@@ -58,8 +58,10 @@ int main() {
         for (int lg = 0; lg <= 5; ++lg) {
           Geometry h = g;
           if (set_z_geometry(h, n1, n2, n3, vs, 1 << lg) && h.zNparts <= cap) z_ok(h, n1, n2, n3, ns, vs, bs);
-          h = g;
-          if (set_x_geometry(h, n1, n2, n3, ns, vs, bs, lg)) x_ok(h, n1, n2, n3, ns, vs, bs);
+          for (bool wide : {false, true}) {
+            h = g;
+            if (set_x_geometry(h, n1, n2, n3, ns, vs, bs, lg, wide)) x_ok(h, n1, n2, n3, ns, vs, bs);
+          }
         }
         for (int lg = 0; lg <= 7; ++lg) {
           Geometry h = g;
