@@ -473,10 +473,14 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
   // S is x-fastest: line (a, t) of the tile is L contiguous values; consecutive
   // lanes copy consecutive x (whole 128-byte lines per warp)
-  auto gline = [&](int ln) { return S + (((long long)r * NS + (ln >> lgT)) * p.inner + c0 + (ln & (TT - 1))) * L; };
+  // element x of tile line ln sits at Sr[goff(ln) + x]: 32-bit offsets from the
+  // tile's base (a replica's ns fields hold fewer than 2^31 values)
+  V *Sr = S + ((long long)r * NS * p.inner + c0) * L;
+  const int fstride = (int)p.inner * L;
+  auto goff = [&](int ln) { return (ln >> lgT) * fstride + (ln & (TT - 1)) * L; };
   for (int e = tid; e < nel; e += nthr) {
     const int x = e & (L - 1), ln = e >> lgL;
-    cp_async_elem(&sm[ln * LP + x], gline(ln) + x);
+    cp_async_elem(&sm[ln * LP + x], Sr + goff(ln) + x);
   }
   cp_async_commit();
   // B tile: one contiguous block of P * npt values, TMA bulk copies issued by
@@ -577,7 +581,7 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   __syncthreads();
   for (int e = tid; e < nel; e += nthr) {
     const int x = e & (L - 1), ln = e >> lgL;
-    gline(ln)[x] = sm[ln * LP + x];
+    Sr[goff(ln) + x] = sm[ln * LP + x];
   }
 }
 
