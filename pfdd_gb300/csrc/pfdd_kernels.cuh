@@ -2,8 +2,9 @@
 // FP64 or FP32 spectral precision).
 //
 // Device data (N = N1*N2*N3, R replicas, ns slip systems):
-//   xi   double2 [R][ns][N]   order parameter, FP64 state (F:4146)
-//   S    T2      [R][ns][N]   spectral work buffer (T = double or float)
+//   xi   double2 [R][ns][N]   order parameter, FP64 state (F:4146), [x][y][z]
+//   S    T2      [R][ns][N]   spectral work buffer (T = double or float), in a
+//                step's context x fastest: [y][z][x] per field
 //   B    T       packed symmetric B(k), P = ns(ns+1)/2 pairs a <= b in
 //                row-major order, stored in the tile order of the fused
 //                x-pass (see BLayout) so each tile streams one contiguous block
@@ -13,7 +14,7 @@
 //   y-forward FFT, x-pass (x-forward FFT -> B(k) contraction -> x-inverse FFT),
 //   y-inverse FFT, z-pass (z-inverse FFT -> Euler update + gamma partials ->
 //   z-forward FFT of the new state).
-// S therefore holds the z-transformed state between steps.
+// S therefore holds the (y,z)-transformed state between steps.
 #pragma once
 #include <climits>
 #include <type_traits>
@@ -88,21 +89,6 @@ template <> struct UpdCoef<float> {
   __device__ float tau(double t) const { return (float)t; }
 };
 
-__device__ __forceinline__ double block_sum(double v, double *red) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
-    for (int i = 0; i < nw; ++i) s += red[i];
-  }
-  return s;
-}
-
 // Exact accumulation of FP64 values in 64-bit fixed point with 2^-44
 // resolution, on the integer pipe (FP64 adds run at 1/58 of the FP32 rate on
 // GB300).  round(d * 2^44) is formed from the bit pattern; |d| must stay below
@@ -139,7 +125,7 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *red) 
 }
 
 // z-pass: TL lines of length L along z (one field), see ZFlags.
-// Shared memory: twiddles [L] | S lines [TL][pitch] (odd pitch) | xi tile
+// Shared memory: twiddles [L] | S lines [TL][pitch] (z_line_pitch) | xi tile
 // [TL][L] double2 (update only).  The FP64 xi lines arrive by TMA bulk copies
 // that overlap the inverse FFT.  Natural layout: the block's lines are
 // consecutive (x, y) pairs, whose S values arrive by cp.async; x-fastest S
@@ -359,11 +345,12 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
     constexpr int L8 = 1 << (LG - 3);
     const int t = tid & (TI - 1), th = tid >> lgTI;
     V *col = base + t;
+    const int in32 = (int)inner;  // a line spans L * inner < 2^31 values
     V v[8];
 #pragma unroll
-    for (int m = 0; m < 8; ++m) v[m] = col[(long long)(th + m * L8) * inner];
+    for (int m = 0; m < 8; ++m) v[m] = col[(th + m * L8) * in32];
     line_fft_io<S, LG, true, true>(v, th, tws, [&](int l) { return &sm[l * pitch + t]; },
-                                   [&](int l) { return &col[(long long)l * inner]; }, true);
+                                   [&](int l) { return &col[l * in32]; }, true);
     return;
   }
   for (int e = tid; e < nel; e += nthr) {
