@@ -123,12 +123,15 @@ struct pfdd_server {
 static void worker_main(pfdd_server *s, Class *c);
 
 // Under s->mu: creates the class of request r if the budget admits it, with
-// as many slots (up to max_slots) as fit.
+// as many slots (up to max_slots) as fit, and at most an eighth of the budget
+// unless one slot needs more: large grids gain nothing from wide batches (their
+// steps are bound by memory bandwidth), and allocating tens of GB for slots
+// that may stay empty delays every class created beside them.
 static Class *try_make_class(pfdd_server *s, const Request &r) {
   const pfdd_request &q = r.spec;
   int slots = s->max_slots;
   size_t need = pfdd_required_bytes(q.n1, q.n2, q.n3, q.ns, slots, s->prec);
-  while (slots > 1 && s->reserved + need > s->budget) {
+  while (slots > 1 && (s->reserved + need > s->budget || need > s->budget / 8)) {
     --slots;
     need = pfdd_required_bytes(q.n1, q.n2, q.n3, q.ns, slots, s->prec);
   }
