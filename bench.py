@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg, print its JSON")
+    ap.add_argument("--no-curve", action="store_true",
+                    help="skip the 1000-step FP32-vs-FP64 error curve of the 128^3 solve")
     ap.add_argument("--batched-steps", type=int, default=100,
                     help="timed steps of the 16-replica batched leg (0 skips it)")
     ap.add_argument("--batched-only", action="store_true", help="run only the batched leg, print its JSON")
@@ -382,6 +384,32 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     }
 
 
+def precision_curve(native, workloads, spec, dev, every=100):
+    """Config 2's report: the FP32-FFT form against the plain FP64 form (which
+    matches the reference's FP64 run) on the same inputs over the whole
+    1000-step ramp, every `every` steps: max |dxi|, the largest |d gamma| so
+    far, that over the largest |gamma| so far (the curve crosses zero, where a
+    pointwise relative error means nothing), and the pointwise one."""
+    x0, b0 = workloads.initial_state(spec)
+    tau = native.spec_tau(spec)
+    ctx = {}
+    for prec in ("fp32", "fp64"):
+        ctx[prec] = native.solver_for(spec, prec, device=dev)
+        ctx[prec].set_state(x0, b0)
+    out, worst, dmax, gmax = [], 0.0, 0.0, 0.0
+    for s0 in range(0, spec.steps, every):
+        g = {p: c.step(tau[s0:s0 + every])[0][:, 0] for p, c in ctx.items()}
+        d = np.abs(g["fp32"] - g["fp64"])
+        worst = max(worst, float(np.max(d / np.abs(g["fp64"]))))
+        dmax, gmax = max(dmax, float(d.max())), max(gmax, float(np.abs(g["fp64"]).max()))
+        dxi = float(np.max(np.abs(ctx["fp32"].get_state() - ctx["fp64"].get_state())))
+        out.append({"step": s0 + every, "max_dxi": dxi, "max_dgamma": dmax, "dgamma_over_max_gamma": dmax / gmax,
+                    "gamma_pointwise_rel_err": worst, "gamma_fp64": float(g["fp64"][-1])})
+    for c in ctx.values():
+        c.close()
+    return out
+
+
 def time_strain(native, workloads, spec, dev, reps=3):
     """pfdd_strain_stress on the solve's initial state (FP64 fields, reference
     strain/stress outputs): wall time per call with the 9+9 fields copied to the
@@ -517,9 +545,12 @@ def run_ours(a):
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline and r64["B"] is not None:
         cpu = cpu_baseline_port(spec, r64["B"])
-    strain = None
+    strain = curve = None
     if dist.world == 1:
         strain = time_strain(native, workloads, spec, dev)
+        if not a.no_curve:
+            curve = {"config1_128c_ns12": precision_curve(native, workloads, spec, dev),
+                     "config0_32c_ns3": precision_curve(native, workloads, workloads.config0(), dev, every=50)}
     batched = None
     if dist.world == 1 and a.batched_steps > 0:
         batched = run_batched(native, workloads, dev, a.batched_steps, max(5, a.batched_steps // 8))
@@ -553,7 +584,8 @@ def run_ours(a):
                   "strain_rel_err_fp32_vs_fp64": strain_err, "strain_err_steps": kk},
         "kernels": kern, "plan": r32["plan"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(r32["launches"]), "launches_per_step": round(launches_per_step, 2),
-        "clocks": r32["clocks"], "strain_stress": strain, "batched": batched, "serving": serving,
+        "clocks": r32["clocks"], "strain_stress": strain, "fp32_vs_fp64_every_100_steps": curve,
+        "batched": batched, "serving": serving,
     }
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
