@@ -233,3 +233,15 @@ def test_fp32_bfly_noncubic_and_batched(native_lib):
         np.testing.assert_array_equal(xb[r], xr)
         xo, go, _ = oracle.solve(sp)
         assert rel(gr, go) <= FP32_GAMMA_RTOL
+
+
+@pytest.mark.parametrize("n", [(16, 1, 16), (1, 16, 32), (16, 16, 1), (2, 4, 8), (512, 2, 2), (2, 2, 512)])
+def test_degenerate_and_long_axes_match_oracle(native_lib, n):
+    """Axes of length 1 (quasi-2D and 1-D grids), tiny grids and 512-long lines, in both forms."""
+    spec = workloads.SolveSpec(n=n, ns=3, steps=12, sigma_max=0.04, noise_seed=13, noise_amp=0.05)
+    xo, go, _ = oracle.solve(spec)
+    x64, g64, _, _ = run_gpu(spec, "fp64")
+    assert np.max(np.abs(x64 - xo)) <= XI_TOL
+    assert rel(g64, go) <= GAMMA_RTOL
+    x32, g32, _, _ = run_gpu(spec, "fp32")
+    assert np.max(np.abs(x32 - xo)) <= 1e-5
