@@ -411,14 +411,16 @@ static void t_end(pfdd_ctx *c, int id) {
   c->tm.used += 2;
 }
 
-// Stockham radices of a line of length n (radix 8 while at least 8 remain).
-static std::string radix_plan(int n) {
+// Stockham radices of a line of length n transformed with nv values per
+// thread (radix nv while at least nv remain, then the remainder).
+static std::string radix_plan(int n, int nv) {
   std::string r;
   int lg = 0;
   while ((1 << lg) < n) ++lg;
   if (lg == 0) return "1";
+  const int lgNV = nv == 16 ? 4 : 3;
   while (lg > 0) {
-    const int k = lg >= 3 ? 3 : lg;
+    const int k = lg >= lgNV ? lgNV : lg;
     r += (r.empty() ? "" : "x") + std::to_string(1 << k);
     lg -= k;
   }
@@ -842,6 +844,8 @@ static ZParams make_zparams(const pfdd_ctx *c) {
 
 static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   const Geometry &g = c->g;
+  const int vs = (int)vsize_of(c->prec), lgx = ilog2(c->n[0]);
+  const int xnv = lgx >= 5 && lgx <= 8 ? xpass_nv(lgx, vs) : 8;  // the x-pass's compiled-in lengths
   char b[768];
   snprintf(b, sizeof b,
            "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld}, "
@@ -849,8 +853,9 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
            "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
            "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": %s}",
            1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, 1 << g.lgTI[0], g.threads[0], g.smem[0],
-           g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0]).c_str(), radix_plan(c->n[1]).c_str(),
-           radix_plan(c->n[2]).c_str(), kGraphSteps, tuning.c_str());
+           g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
+           radix_plan(c->n[1], fft_nv(ilog2(c->n[1]))).c_str(), radix_plan(c->n[2], zpass_nv(ilog2(c->n[2]), vs)).c_str(),
+           kGraphSteps, tuning.c_str());
   return b;
 }
 

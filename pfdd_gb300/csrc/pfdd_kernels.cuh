@@ -142,7 +142,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
   V *tws = reinterpret_cast<V *>(smraw);
   V *sm = tws + L;
   double2 *xs = reinterpret_cast<double2 *>(smraw + ((((size_t)L + (size_t)TL * P) * sizeof(V) + 15) & ~(size_t)15));
-  const int E = L >= 8 ? 8 : L, team = L / E;
+  constexpr int NV = zpass_nv(LG, (int)sizeof(V));
+  const int E = L >= NV ? NV : L, team = L / E;
   const long long line0 = (long long)blockIdx.x * TL;
   const long long rf = line0 / p.lines_per_field;
   const int r = (int)(rf / p.ns), a = (int)(rf % p.ns);
@@ -201,21 +202,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
   const bool act = th < team;
   auto line = [&](int l) { return &sm[t * P + l]; };
   auto gline = [&](int l) { return &Sf[sb + t + l * sk]; };  // S element z = l of line t
-  V v[8];
+  V v[NV];
   if (p.flags & Z_INV) {
     if constexpr (kIO) {
       if (direct && !(p.flags & Z_SRC_XI)) {
-        constexpr int L8 = L >> 3;
+        constexpr int LV = L / NV;
         if (act) {
 #pragma unroll
-          for (int m = 0; m < 8; ++m) v[m] = *gline(th + m * L8);
+          for (int m = 0; m < NV; ++m) v[m] = *gline(th + m * LV);
         }
-        line_fft_io<+1, LG, true, false>(v, th, tws, line, line, act);
+        line_fft_io<+1, LG, true, false, NV>(v, th, tws, line, line, act);
       } else {
-        line_fft<+1, LG>(th, lgL, tws, line, act);
+        line_fft<+1, LG, NV>(th, lgL, tws, line, act);
       }
     } else {
-      line_fft<+1, LG>(th, lgL, tws, line, act);
+      line_fft<+1, LG, NV>(th, lgL, tws, line, act);
     }
   }
 
@@ -301,11 +302,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
 
   if constexpr (kIO) {
     if (direct) {  // forward transform, last stage straight to S
-      line_fft_io<-1, LG, false, true>(v, th, tws, line, gline, act);
+      line_fft_io<-1, LG, false, true, NV>(v, th, tws, line, gline, act);
       return;
     }
   }
-  if (p.flags & Z_FWD) line_fft<-1, LG>(th, lgL, tws, line, act);
+  if (p.flags & Z_FWD) line_fft<-1, LG, NV>(th, lgL, tws, line, act);
   if (p.flags & Z_STORE) {
     __syncthreads();
     if (xf) {
@@ -342,15 +343,15 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
     // consecutive columns: coalesced), the last stage straight back; shared
     // memory only between stages.  The first stage uses no twiddles, and the
     // barrier after it orders the twiddle table before the second.
-    constexpr int L8 = 1 << (LG - 3);
+    constexpr int NV = fft_nv(LG), LV = (1 << LG) / NV;
     const int t = tid & (TI - 1), th = tid >> lgTI;
     V *col = base + t;
     const int in32 = (int)inner;  // a line spans L * inner < 2^31 values
-    V v[8];
+    V v[NV];
 #pragma unroll
-    for (int m = 0; m < 8; ++m) v[m] = col[(th + m * L8) * in32];
-    line_fft_io<S, LG, true, true>(v, th, tws, [&](int l) { return &sm[l * pitch + t]; },
-                                   [&](int l) { return &col[l * in32]; }, true);
+    for (int m = 0; m < NV; ++m) v[m] = col[(th + m * LV) * in32];
+    line_fft_io<S, LG, true, true, NV>(v, th, tws, [&](int l) { return &sm[l * pitch + t]; },
+                                       [&](int l) { return &col[l * in32]; }, true);
     return;
   }
   for (int e = tid; e < nel; e += nthr) {
@@ -360,7 +361,7 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  const int E = L >= 8 ? 8 : L, team = L / E;
+  const int E = L >= 8 ? 8 : L, team = L / E;  // LG < 3 here: one thread per line
   const int t = tid & (TI - 1), th = tid >> lgTI;  // consecutive lanes on consecutive lines
   const bool act = th < team;
   line_fft<S, LG>(th, lgL, tws, [&](int l) { return &sm[l * pitch + t]; }, act);
@@ -455,7 +456,8 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nel = (NS * L) << lgT;
   auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + x; };
-  const int E = L >= 8 ? 8 : L, team = L / E, teams = nthr / team;
+  constexpr int NV = LG >= 0 ? xpass_nv(LG, (int)sizeof(V)) : 8;
+  const int E = L >= NV ? NV : L, team = L / E, teams = nthr / team;
   const int lines = NS << lgT;
   const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
   // S is x-fastest: line (a, t) of the tile is L contiguous values; consecutive
@@ -486,7 +488,7 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   __syncthreads();
   for (int l0 = 0; l0 < lines; l0 += teams) {
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-    line_fft<-1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+    line_fft<-1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
   }
   if (bulk) mbar_wait(&bbar, 0, p.err);
   __syncthreads();
@@ -563,7 +565,7 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   __syncthreads();
   for (int l0 = 0; l0 < lines; l0 += teams) {
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-    line_fft<+1, LG>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+    line_fft<+1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
   }
   __syncthreads();
   for (int e = tid; e < nel; e += nthr) {

@@ -38,6 +38,16 @@ inline int ilog2(long long v) {
   return l;
 }
 
+// threads per line (team) of the strided passes and the z-pass, which have
+// every line length compiled in, and of the fused x-pass, which has N1 =
+// 32..256 compiled in and runs other lengths with 8 values per thread
+inline int line_team(int L) { return L / std::min(fft_nv(ilog2(L)), L); }
+inline int z_line_team(int L, size_t vsize) { return L / std::min(zpass_nv(ilog2(L), (int)vsize), L); }
+inline int x_line_team(int n1, size_t vsize) {
+  const int lg = ilog2(n1);
+  return n1 / std::min(lg >= 5 && lg <= 8 ? xpass_nv(lg, (int)vsize) : 8, n1);
+}
+
 // dynamic shared memory a kernel may opt into (227 KB per block on GB300,
 // less the kernels' few hundred bytes of static shared memory)
 constexpr size_t kMaxDynSmem = 226 * 1024;
@@ -75,7 +85,7 @@ inline int z_line_pitch(int L, int TL, size_t vsize) {
 
 // z-pass with TL lines per block (the x-fastest layout needs TL <= N1).
 inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, int TL) {
-  const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
+  const int L3 = n3, team3 = z_line_team(L3, vsize);
   const long long lines = (long long)n1 * n2;
   if (TL < 1 || TL > lines || (g.xfast && TL > n1) || (long long)TL * team3 > kThreads) return false;
   g.zTL = TL;
@@ -90,7 +100,7 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
 
 // Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.
 inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, int lgTI, size_t vsize) {
-  const int E = std::min(8, L), team = L / E;
+  const int team = line_team(L);
   const int TI = 1 << lgTI;
   if (TI > inner || (long long)TI * team > kThreads) return false;  // fft_strided_kernel launch bounds
   g.lgTI[ax] = lgTI;
@@ -114,7 +124,7 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
   const int pitch = line_pitch(n1);
   const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize);
   if (smem > kMaxDynSmem) return false;
-  const int team = n1 / std::min(8, n1), lines = ns << lgT, npt = n1 << lgT;
+  const int team = x_line_team(n1, vsize), lines = ns << lgT, npt = n1 << lgT;
   const int unit = std::max(32, team);
   const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
   if (unit > cap) return false;
@@ -139,7 +149,7 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
 inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, bool xfast = false) {
   Geometry g;
   g.xfast = xfast;
-  const int L3 = n3, E3 = std::min(8, L3), team3 = L3 / E3;
+  const int L3 = n3, team3 = z_line_team(L3, vsize);
   const long long lines = (long long)n1 * n2;
   int TL = std::max(1, kThreads / team3);
   while ((long long)TL > lines || (xfast && TL > n1)) TL >>= 1;  // x-fastest: a block's lines share y
@@ -147,7 +157,7 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
   const int Ls[2] = {n2, n1};
   const long long inner[2] = {xfast ? (long long)n3 * n1 : (long long)n3, (long long)n2 * n3};
   for (int ax = 0; ax < 2; ++ax) {
-    const int L = Ls[ax], E = std::min(8, L), team = L / E;
+    const int L = Ls[ax], team = line_team(L);
     int TI = std::max(1, kThreads / team);
     while ((long long)TI > inner[ax]) TI >>= 1;
     set_strided_geometry(g, ax, L, inner[ax], ilog2(TI), vsize);

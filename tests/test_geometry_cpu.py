@@ -15,9 +15,20 @@ HARNESS = r"""
 #include "pfdd_launch.h"
 using namespace pfdd;
 static int bad = 0, checked = 0;
+// threads per line as the kernels compute it: 16 values per thread for lines
+// of 16, 128 and 256 in the strided passes, the FP64 z-pass and the FP32
+// x-pass (whose compiled-in lengths are 32..256), else 8; lines shorter than
+// that: one thread.  kind: 0 strided, 1 z-pass, 2 x-pass.
+static int team_of(int L, int kind, size_t vs) {
+  bool nv16 = L == 16 || L == 128 || L == 256;
+  if (kind == 1 && vs == 8) nv16 = false;
+  if (kind == 2 && (vs == 16 || L == 16)) nv16 = false;
+  const int nv = nv16 ? 16 : 8;
+  return L < nv ? 1 : L / nv;
+}
 #define CHECK(c, what) do { if (!(c)) { ++bad; std::printf("FAIL %s n=%dx%dx%d ns=%d v=%zu b=%zu\n", what, n1, n2, n3, ns, vs, bs); } } while (0)
 static void z_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
-  const int team = n3 / (n3 < 8 ? n3 : 8);
+  const int team = team_of(n3, 1, vs);
   CHECK((g.zTL & (g.zTL - 1)) == 0 && g.zTL <= n1 && n1 % g.zTL == 0, "z lines");
   CHECK(g.zThreads == g.zTL * team && g.zThreads <= kThreads, "z threads");
   CHECK(g.zSmem <= kMaxDynSmem && g.zPitch >= n3 + 1, "z smem/pitch");
@@ -25,13 +36,13 @@ static void z_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, s
 }
 static void y_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
   const long long inner = (long long)n3 * n1;
-  const int team = n2 / (n2 < 8 ? n2 : 8);
+  const int team = team_of(n2, 0, vs);
   const int TI = 1 << g.lgTI[0];
   CHECK(TI <= inner && inner % TI == 0 && g.tiles[0] * TI == inner, "y tiles");
   CHECK(g.threads[0] == TI * team && g.threads[0] <= kThreads && g.smem[0] <= kMaxDynSmem, "y threads/smem");
 }
 static void x_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
-  const int team = n1 / (n1 < 8 ? n1 : 8);
+  const int team = team_of(n1, 2, vs);
   const int cap = (vs == 16 || bs == 0) ? 256 : 384;
   CHECK(g.xTiles << g.xLgT == (long long)n2 * n3, "x tiles");
   CHECK(g.xThreads >= team && g.xThreads % team == 0 && g.xThreads <= cap, "x threads");
