@@ -320,7 +320,7 @@ struct KTiming {
 
 struct pfdd_ctx {
   int n[3] = {0, 0, 0};
-  int ns = 0, nrep = 0, prec = 0, dev = 0;
+  int ns = 0, nrep = 0, prec = 0, dev = 0, nsm = 1;
   long long N = 0;
   cudaStream_t st = nullptr;
   void *S = nullptr;
@@ -489,6 +489,7 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   c->ns = ns; c->nrep = nrep; c->prec = precision; c->dev = device;
   c->N = (long long)n1 * n2 * n3;
   CK(c, cudaSetDevice(device));
+  CK(c, cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision), /*xfast=*/true);
   if (!c->g.valid)
@@ -640,13 +641,17 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
     BFlyParams &bf = c->bf;
     bf.n2 = c->n[1]; bf.n3 = c->n[2]; bf.lgN3 = ilog2(c->n[2]);
     bf.d[0] = (float)d1; bf.d[1] = (float)d2; bf.d[2] = (float)d3;
-    bf.mu = (float)hp.mu; bf.ll = (float)hp.ll; bf.mup = (float)hp.mup; bf.mu_inv = (float)hp.mu_inv;
-    int q = 0;
-    for (int a = 0; a < c->ns; ++a) {
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) bf.sig[a][i][j] = (float)hp.sig[a][i][j];
-      for (int b = a; b < c->ns; ++b, ++q) bf.E[q] = (float)hp.E[a][b];
-    }
+    bf.mu = (float)hp.mu; bf.ll = (float)hp.ll; bf.mup = (float)hp.mup;
+    static const int comp[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+    for (int a = 0; a < c->ns; ++a)
+      for (int cc = 0; cc < 6; ++cc) {
+        const int i = comp[cc][0], j = comp[cc][1];
+        const double m = i == j ? 1.0 : 2.0;
+        const double se = 0.5 * (eps[(a * 3 + i) * 3 + j] + eps[(a * 3 + j) * 3 + i]);  // eps_a : W = sym(eps_a) : W
+        bf.sig6[a][cc] = (float)hp.sig[a][i][j];
+        bf.pe6[a][cc] = (float)(m * se * hp.mu_inv);
+        bf.qs6[a][cc] = (float)(-m * hp.sig[a][i][j] * hp.mu_inv);
+      }
     c->hasB = true;
     return PFDD_OK;
   }
@@ -771,7 +776,13 @@ static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
   const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
   t_begin(c);
-  cudaError_t e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp);
+  cudaError_t e;
+  if (c->g.zPipe > 0 && flags == (Z_INV | Z_UPDATE | Z_FWD | Z_STORE)) {
+    const long long grid = std::min<long long>(blocks, (long long)c->nsm * c->g.zPipe);
+    e = launch_zpass_pipe(c->g.lgL3, (unsigned)grid, c->g.zThreads, c->g.zPipeSmem, c->st, zp, (int)blocks);
+  } else {
+    e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp);
+  }
   t_end(c, (flags & Z_UPDATE) ? K_Z_STEP : K_Z_PROLOGUE);
   return e;
 }
@@ -806,7 +817,9 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   t_begin(c);
   xp.bf = c->bf;
   xp.err = c->errflag;
-  cudaError_t e = c->prec == PFDD_FFT_FP32_BFLY
+  cudaError_t e = c->g.xWarp
+                      ? launch_x_warp_f32(c->ns, c->prec == PFDD_FFT_FP32_BFLY, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
+                  : c->prec == PFDD_FFT_FP32_BFLY
                       ? launch_x_fused_f32_bfly(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
                       : (std::is_same<T, float>::value
                              ? launch_x_fused_f32(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
@@ -846,25 +859,25 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   const Geometry &g = c->g;
   const int vs = (int)vsize_of(c->prec), lgx = ilog2(c->n[0]);
   const int xnv = lgx >= 5 && lgx <= 8 ? xpass_nv(lgx, vs) : 8;  // the x-pass's compiled-in lengths
-  char b[768];
+  char b[1024];  // the fixed part; the autotune timings follow
   snprintf(b, sizeof b,
-           "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld}, "
+           "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld, \"warp_teams\": %d}, "
            "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
-           "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
-           "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": %s}",
-           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, 1 << g.lgTI[0], g.threads[0], g.smem[0],
-           g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
+           "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu, \"pipelined_ctas_per_sm\": %d}, "
+           "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": ",
+           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp, 1 << g.lgTI[0], g.threads[0], g.smem[0],
+           g.tiles[0], g.zTL, g.zThreads, g.zPipe ? g.zPipeSmem : g.zSmem, g.zPipe, radix_plan(c->n[0], xnv).c_str(),
            radix_plan(c->n[1], fft_nv(ilog2(c->n[1]))).c_str(), radix_plan(c->n[2], zpass_nv(ilog2(c->n[2]), vs)).c_str(),
-           kGraphSteps, tuning.c_str());
-  return b;
+           kGraphSteps);
+  return std::string(b) + tuning + "}";
 }
 
 // Tuned plans by grid shape (N1, N2, N3, ns, precision, device): a process
 // times each shape once; later contexts of the shape (serving classes, batch
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
-  int zTL, xLgT, yLgTI;
-  bool xWide;
+  int zTL, zPipe, xLgT, yLgTI;
+  bool xWide, xWarp;
   std::string timings;
 };
 static std::mutex g_plan_mu;
@@ -884,9 +897,11 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,x=<tile columns>,y=<tile columns>" pins the plan (each
-  // entry optional, ignored when it does not fit) instead of timing it, e.g.
-  // to profile the plan a timed run chose (a profiler distorts the timings)
+  // PFDD_PLAN="z=<lines>,p=<CTAs per SM>,x=<tile columns>,w=<0|1>,y=<tile columns>"
+  // pins the plan (each entry optional, ignored when it does not fit; p, the
+  // pipelined z-pass, after z; w=1, the warp-team x-pass, after x) instead of
+  // timing it, e.g. to profile the plan a timed run chose (a profiler distorts
+  // the timings)
   if (const char *pin = std::getenv("PFDD_PLAN")) {
     const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
     for (const char *q = pin; *q;) {
@@ -895,7 +910,9 @@ static pfdd_status autotune(pfdd_ctx *c) {
       if (std::sscanf(q, "%c=%d", &key, &v) == 2 && v > 0) {
         Geometry g = c->g;
         const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v) && g.zNparts <= c->zparts_cap
+                        : key == 'p' ? set_z_pipe(g, c->n[2], vs, v)
                         : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v))
+                        : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false, v == 1)
                         : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs)
                                      : false;
         if (ok) c->g = g;
@@ -917,7 +934,9 @@ static pfdd_status autotune(pfdd_ctx *c) {
       if (it != g_plans.end()) {
         Geometry g = c->g;
         if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
-            set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide) &&
+            set_z_pipe(g, c->n[2], vs, it->second.zPipe) &&
+            set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide,
+                           it->second.xWarp) &&
             (c->n[1] == 1 ||
              set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs))) {
           c->g = g;
@@ -961,9 +980,13 @@ static pfdd_status autotune(pfdd_ctx *c) {
     fill_u64_kernel<<<1216, kThreads, 0, c->st>>>(reinterpret_cast<unsigned long long *>(c->xi),
                                                   (long long)c->ns * c->N * 2, 0x3fe0000000000000ull);
     cudaMemsetAsync(c->tau, 0, (size_t)c->nrep * c->ns * sizeof(double), c->st);
-    for (int lgTL = 0; lgTL <= 5; ++lgTL) {
+    // each line count plain and pipelined with 2..4 persistent CTAs per SM
+    // (key "<lines>p<CTAs per SM>"); both compute every tile identically
+    for (int cand = 0; cand <= 6 * 4 - 1; ++cand) {
+      const int lgTL = cand >> 2, cps = (cand & 3) == 0 ? 0 : (cand & 3) + 1;
       Geometry g = c->g;
       if (!set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, 1 << lgTL) || g.zNparts > c->zparts_cap) continue;
+      if (!set_z_pipe(g, c->n[2], vs, cps)) continue;
       c->g = g;
       ZParams zp = make_zparams(c);
       zp.step_ctr = nullptr;
@@ -971,21 +994,26 @@ static pfdd_status autotune(pfdd_ctx *c) {
       const double us = time_us([&] { return ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
-      snprintf(b, sizeof b, "%s\"%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, us);
+      if (cps)
+        snprintf(b, sizeof b, "%s\"%dp%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, cps, us);
+      else
+        snprintf(b, sizeof b, "%s\"%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, us);
       zs += b;
     }
     c->g = best;
     bt = 1e30;
-    for (int cand = 0; cand <= 13; ++cand) {
-      const int lgT = cand >> 1;
-      const bool wide = cand & 1;
+    // tile widths 1..64, each with the block-team kernel (plain and wide) and
+    // the warp-team kernel (key suffix "v"); all compute the same bits
+    for (int cand = 0; cand <= 3 * 7 - 1; ++cand) {
+      const int lgT = cand / 3, form = cand % 3;
+      const bool wide = form == 1, warp = form == 2;
       Geometry g = c->g;
-      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide)) continue;
+      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide, warp)) continue;
       c->g = g;
       const double us = time_us([&] { return launch_x_fused<T>(c); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
-      snprintf(b, sizeof b, "%s\"%d%s\": %.1f", xs.empty() ? "" : ", ", 1 << lgT, wide ? "w" : "", us);
+      snprintf(b, sizeof b, "%s\"%d%s\": %.1f", xs.empty() ? "" : ", ", 1 << lgT, wide ? "w" : (warp ? "v" : ""), us);
       xs += b;
     }
     c->g = best;
@@ -1017,7 +1045,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
              ys + "}}";
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.xWide, tuning};
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.zPipe, c->g.xLgT, c->g.lgTI[0], c->g.xWide, c->g.xWarp, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }

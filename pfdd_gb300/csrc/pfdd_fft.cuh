@@ -229,7 +229,11 @@ __device__ __forceinline__ void line_fft(int th, int lgL_rt, const V *tw, Addr s
 // shared-memory read.  OUT_DIRECT: the last stage writes through `out` (e.g.
 // global memory, natural order) instead of `sm`, and no barrier follows it.
 // `sm` holds the line between stages; every thread of the block must call it.
-template <int S, int LG, bool IN_REGS, bool OUT_DIRECT, int NV = 8, typename V, typename AddrS, typename AddrO>
+// WARP: the team's threads sit in one warp (the line lives in the warp's own
+// part of shared memory), so the stages synchronise the warp, not the block;
+// every lane of a warp that calls it must call it.
+template <int S, int LG, bool IN_REGS, bool OUT_DIRECT, int NV = 8, bool WARP = false, typename V, typename AddrS,
+          typename AddrO>
 __device__ __forceinline__ void line_fft_io(V *v, int th, const V *tw, AddrS sm, AddrO out, bool active) {
   constexpr int lgNV = NV == 16 ? 4 : 3;
   static_assert(LG >= lgNV, "line_fft_io needs L >= NV");
@@ -242,13 +246,17 @@ __device__ __forceinline__ void line_fft_io(V *v, int th, const V *tw, AddrS sm,
 #pragma unroll
         for (int m = 0; m < NV; ++m) v[m] = *sm(th + m * LV);
       }
-      __syncthreads();  // every read of this stage precedes its in-place writes
+      if (WARP) __syncwarp();  // every read of this stage precedes its in-place writes
+      else __syncthreads();
     }
     if (active) {
       if (OUT_DIRECT && st == NST - 1) stockham_plan_stage<S, NV>(v, th, LG, st, tw, out);
       else stockham_plan_stage<S, NV>(v, th, LG, st, tw, sm);
     }
-    if (!(OUT_DIRECT && st == NST - 1)) __syncthreads();
+    if (!(OUT_DIRECT && st == NST - 1)) {
+      if (WARP) __syncwarp();
+      else __syncthreads();
+    }
   }
 }
 

@@ -124,6 +124,57 @@ __device__ __forceinline__ long long block_sum_i64(long long v, long long *red) 
   return s;
 }
 
+// The FP32-FFT form's Euler update of one z-pass tile (TL lines of L = 2^LG,
+// nel = TL*L points, element e = line * L + z): the force from the FP32
+// spectrum sm (line pitch P), the FP64 state from xsb (the tile in shared
+// memory, as bit patterns).  Writes the evolved state to xg (the field's xi)
+// and its FP32 copy back to sm; returns the tile's exact fixed-point sum of
+// Re xi (big: see to_fixed_bits).  The FP64 state stays in integer registers;
+// FP64 arithmetic is exactly the two subtractions (the compiler otherwise
+// routes 64-bit register moves through the FP64 pipe).  kGeneral: pinned
+// points or a stress field (read per point); otherwise every point evolves
+// under the tile's one stress value.
+template <bool kGeneral, int LG>
+__device__ __forceinline__ long long update_tile_f32(const ZParams &p, const UpdCoef<float> &k, float ctau0, double tv,
+                                                     int a, long long fbase, int lb, int ls, int nel, int P,
+                                                     float2 *sm, const ulonglong2 *xsb, ulonglong2 *xg, bool &big) {
+  constexpr int L = 1 << LG;
+  long long acc = 0;
+#pragma unroll 2
+  for (int e = threadIdx.x; e < nel; e += blockDim.x) {
+    float2 *sp = &sm[(e >> LG) * P + (e & (L - 1))];
+    ulonglong2 xb = xsb[e];
+    const int pt = lb + (e >> LG) * ls + (e & (L - 1));
+    bool evolve = true;
+    float ctau = ctau0;
+    if constexpr (kGeneral) {
+      if (p.bc) {
+        const long long bit = fbase + pt;
+        evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
+      }
+      if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
+    }
+    if (evolve) {
+      const float2 f = *sp;
+      const float xr = f64bits_to_f32_fast(xb.x);
+      const float s = sinpif(2.0f * xr);
+      const float dre = k.cd2 * (k.uq2 * f.x * k.inv_n + k.asf_pi * s - ctau);
+      const float dim = k.uq2cd2 * (f.y * k.inv_n);
+      xb.x = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.x) -
+                                                      __longlong_as_double((long long)f32_to_f64bits_fast(dre)));
+      xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
+                                                      __longlong_as_double((long long)f32_to_f64bits_fast(dim)));
+      xg[pt] = xb;
+    }
+    acc += to_fixed_bits(xb.x, big);
+    float2 o;
+    o.x = f64bits_to_f32_fast(xb.x);
+    o.y = f64bits_to_f32_fast(xb.y);
+    *sp = o;
+  }
+  return acc;
+}
+
 // z-pass: TL lines of length L along z (one field), see ZFlags.
 // Shared memory: twiddles [L] | S lines [TL][pitch] (z_line_pitch) | xi tile
 // [TL][L] double2 (update only).  The FP64 xi lines arrive by TMA bulk copies
@@ -230,50 +281,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
     long long acc = 0;
     bool big = false;
     if constexpr (sizeof(V) == sizeof(float2)) {
-      // FP32-FFT form: the FP64 state stays in integer registers as bit
-      // patterns; FP64 arithmetic is exactly the two subtractions (the
-      // compiler otherwise routes 64-bit register moves through the FP64 pipe).
       const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xs);
       ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(xif);
-      // general: pinned points or a stress field (read per point); otherwise
-      // every point evolves under the block's one stress value
-      auto update = [&](auto general) {
-        constexpr bool kGeneral = decltype(general)::value;
-#pragma unroll 2
-        for (int e = tid; e < nel; e += nthr) {
-          V *sp = &sm[sidx(e)];
-          ulonglong2 xb = xsb[e];
-          const int pt = lb + (e >> lgL) * ls + (e & (L - 1));
-          bool evolve = true;
-          float ctau = ctau0;
-          if constexpr (kGeneral) {
-            if (p.bc) {
-              const long long bit = fbase + pt;
-              evolve = ((p.bc[bit >> 5] >> (bit & 31)) & 1u) == 0u;
-            }
-            if (p.tau_field) ctau = k.tau((p.tau_field[(long long)a * p.N + pt] * tv) / p.dslip[a]);
-          }
-          if (evolve) {
-            const float2 f = *sp;
-            const float xr = f64bits_to_f32_fast(xb.x);
-            const float s = sinpif(2.0f * xr);
-            const float dre = k.cd2 * (k.uq2 * f.x * k.inv_n + k.asf_pi * s - ctau);
-            const float dim = k.uq2cd2 * (f.y * k.inv_n);
-            xb.x = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.x) -
-                                                            __longlong_as_double((long long)f32_to_f64bits_fast(dre)));
-            xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
-                                                            __longlong_as_double((long long)f32_to_f64bits_fast(dim)));
-            xg[pt] = xb;
-          }
-          acc += to_fixed_bits(xb.x, big);
-          V o;
-          o.x = f64bits_to_f32_fast(xb.x);
-          o.y = f64bits_to_f32_fast(xb.y);
-          *sp = o;
-        }
-      };
-      if (p.bc || p.tau_field) update(std::true_type{});
-      else update(std::false_type{});
+      if (p.bc || p.tau_field)
+        acc = update_tile_f32<true, LG>(p, k, ctau0, tv, a, fbase, lb, ls, nel, P, sm, xsb, xg, big);
+      else
+        acc = update_tile_f32<false, LG>(p, k, ctau0, tv, a, fbase, lb, ls, nel, P, sm, xsb, xg, big);
     } else {
       for (int e = tid; e < nel; e += nthr) {
         V *sp = &sm[sidx(e)];
@@ -317,6 +330,130 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
     } else {
       for (int e = tid; e < nel; e += nthr) Sf[sb + e] = sm[sidx(e)];
     }
+  }
+}
+
+// Shared-memory bytes of the pipelined z-pass: twiddles | two S tiles [TL][P]
+// (16-byte aligned) | two FP64 state tiles [TL][L].
+__host__ __device__ __forceinline__ size_t zpipe_smem(int L, int TL, int P, size_t vsize) {
+  return ((((size_t)L + 2 * (size_t)TL * P) * vsize + 15) & ~(size_t)15) + 2 * (size_t)TL * L * 16;
+}
+
+// Pipelined z-pass of the FP32-FFT form for the step's x-fastest S: inverse
+// z-FFT, Euler update with gamma partials, forward z-FFT, for tiles of TL
+// lines (x0..x0+TL-1, y) of one field, exactly as zpass_kernel's block `tile`
+// computes them (same instructions per line and point, same partial slot).
+// Persistent CTAs take tiles blockIdx.x, + gridDim.x, ...; while one tile is
+// transformed and updated, the S values (cp.async, TL-element runs) and FP64
+// state lines (TMA bulk copies) of the CTA's next tile stream into the other
+// half of a double buffer, so the loads of every tile but the first overlap
+// compute.  Tiles of idle replicas are skipped.
+template <int LG>
+__global__ void __launch_bounds__(256, 2) zpass_pipe_kernel(ZParams p, int ntiles) {
+  using V = float2;
+  static_assert(LG >= 3, "the pipelined z-pass needs L >= 8");
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ long long red[32];
+  __shared__ __align__(8) uint64_t xbar[2];  // completion of the FP64 state tiles
+  constexpr int L = 1 << LG, NV = zpass_nv(LG, (int)sizeof(V)), team = L / NV;
+  const int TL = p.TL, P = p.pitch, lgTL = p.lgTL;
+  const int nel = TL << LG, tid = threadIdx.x, nthr = blockDim.x;
+  V *tws = reinterpret_cast<V *>(smraw);
+  V *sbuf = tws + L;  // [2][TL][P]
+  double2 *xbuf = reinterpret_cast<double2 *>(smraw + ((((size_t)L + 2 * (size_t)TL * P) * sizeof(V) + 15) &
+                                                       ~(size_t)15));  // [2][TL * L]
+  const int xblocks = p.n1 >> lgTL;
+  const int ls = p.n2 * L;  // xi stride between the tile's lines
+  const int step = p.step_ctr ? *p.step_ctr : p.step;
+  // tile -> field rf = r*ns + a, xi offset lb of its first line, S offset sb
+  struct Tile {
+    long long rf;
+    int lb, sb, part;
+  };
+  auto tile_of = [&](int tile) {
+    const long long line0 = (long long)tile * TL;
+    Tile q;
+    q.rf = line0 / p.lines_per_field;
+    const int lf0 = (int)(line0 - q.rf * p.lines_per_field);
+    const int bf = lf0 >> lgTL, x0 = (bf % xblocks) << lgTL, yj = bf / xblocks;
+    q.lb = (x0 * p.n2 + yj) * L;
+    q.sb = yj * L * p.n1 + x0;
+    q.part = lf0 >> lgTL;
+    return q;
+  };
+  auto live = [&](int tile) {
+    if (!p.active) return true;
+    const long long rf = (long long)tile * TL / p.lines_per_field;
+    return p.active[rf / p.ns] != 0;
+  };
+  auto next_live = [&](int tile) {
+    while (tile < ntiles && !live(tile)) tile += gridDim.x;
+    return tile;
+  };
+  // loads of a tile into buffer b: S by cp.async (consecutive lanes on
+  // consecutive x), the FP64 lines by one thread's bulk copies
+  auto issue = [&](int tile, int b) {
+    const Tile q = tile_of(tile);
+    V *Sb = sbuf + b * TL * P;
+    const V *Sf = reinterpret_cast<const V *>(p.S) + q.rf * p.N;
+    for (int e = tid; e < nel; e += nthr) {
+      const int t = e & (TL - 1), z = e >> lgTL;
+      cp_async_elem(&Sb[t * P + z], &Sf[q.sb + t + z * p.n1]);
+    }
+    cp_async_commit();
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive_expect_tx(&xbar[b], (unsigned)nel * 16u);
+      const double2 *xif = p.xi + q.rf * p.N;
+      for (int t = 0; t < TL; ++t) bulk_copy(xbuf + b * nel + (t << LG), xif + q.lb + t * ls, (unsigned)L * 16u, &xbar[b]);
+    }
+  };
+  if (tid == 0) {
+    mbar_init(&xbar[0], 1);
+    mbar_init(&xbar[1], 1);
+  }
+  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  __syncthreads();  // barriers initialised before any thread waits on them
+  const int t = tid & (TL - 1), th = tid >> lgTL;  // consecutive lanes on consecutive lines
+  const bool act = th < team;
+  int cur = next_live(blockIdx.x);
+  if (cur < ntiles) issue(cur, 0);
+  for (int it = 0; cur < ntiles; ++it) {
+    const int b = it & 1;
+    const int nxt = next_live(cur + gridDim.x);
+    // buffer b ^ 1 is free: every read of it (the previous tile's forward FFT
+    // and update) preceded a barrier this thread has passed
+    if (nxt < ntiles) {
+      issue(nxt, b ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const Tile q = tile_of(cur);
+    const int a = (int)(q.rf % p.ns), r = (int)(q.rf / p.ns);
+    V *sm = sbuf + b * TL * P;
+    V *Sf = reinterpret_cast<V *>(p.S) + q.rf * p.N;
+    auto line = [&](int l) { return &sm[t * P + l]; };
+    auto gline = [&](int l) { return &Sf[q.sb + t + l * p.n1]; };
+    line_fft<+1, LG, NV>(th, LG, tws, line, act);
+    mbar_wait(&xbar[b], (unsigned)(it >> 1) & 1u, p.err);
+    const UpdCoef<float> k(p, a);
+    const double tv = p.tau[((long long)step * p.R + r) * p.ns + a];
+    const float ctau0 = k.tau(tv);
+    bool big = false;
+    const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xbuf + b * nel);
+    ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(p.xi + q.rf * p.N);
+    const long long acc =
+        (p.bc || p.tau_field) ? update_tile_f32<true, LG>(p, k, ctau0, tv, a, q.rf * p.N, q.lb, ls, nel, P, sm, xsb, xg, big)
+                              : update_tile_f32<false, LG>(p, k, ctau0, tv, a, q.rf * p.N, q.lb, ls, nel, P, sm, xsb, xg, big);
+    const long long sum = block_sum_i64(acc, red);
+    const int anybig = __syncthreads_or(big);
+    if (tid == 0) p.part[((long long)step * p.R * p.ns + q.rf) * p.nparts + q.part] = anybig ? LLONG_MIN : sum;
+    __syncthreads();
+    V v[NV];
+    line_fft_io<-1, LG, false, true, NV>(v, th, tws, line, gline, act);  // last stage straight to S
+    cur = nxt;
   }
 }
 
@@ -385,13 +522,17 @@ __host__ __device__ __forceinline__ long long b_index(const BLayout &bl, int p, 
   return (tile * bl.P + p) * ((long long)bl.L << bl.lgT) + t * bl.L + x;
 }
 
-// Constants of the closed-form B(k) for the x-pass that evaluates B in FP32
-// registers instead of streaming a stored table (see x_fused_kernel, BFLY).
+// Constants of the closed-form B(k) for the x-pass that evaluates the
+// contraction in FP32 registers instead of streaming a stored table (see
+// x_fused_kernel, BFLY).  Symmetric tensors as six components c = xx, yy, zz,
+// xy, xz, yz; m_c = 1 (diagonal) or 2 (off-diagonal) folds the double
+// contraction of two symmetric tensors into six products.
 struct BFlyParams {
   int n2, n3, lgN3;
-  float d[3], mu, ll, mup, mu_inv;
-  float sig[kMaxNs][3][3];                 // sigma_a = C : eps_a
-  float E[kMaxNs * (kMaxNs + 1) / 2];      // eps_a : C : eps_b, packed pairs a <= b
+  float d[3], mu, ll, mup;
+  float sig6[kMaxNs][6];  // sigma_b = C : eps_b
+  float pe6[kMaxNs][6];   // m_c sym(eps_a)_c / mu
+  float qs6[kMaxNs][6];   // -m_c sigma_a,c / mu
 };
 
 struct XParams {
@@ -414,6 +555,113 @@ __device__ __forceinline__ float frec_f(int i, int n, float d) {
   return v;
 }
 
+// k-space contraction of one point, S_a <- sum_b B_ab S_b (F:4609-4629, b
+// ascending), with the point's B(k) in the shared-memory tile Bs (P pairs a <=
+// b, npt points each).  at(a) is the point's value of field a (read, then
+// overwritten).  IN_REGS keeps the NS inputs in registers.
+template <typename T, int NS, bool IN_REGS, typename At>
+__device__ __forceinline__ void contract_table(const T *Bs, int npt, int q, At at) {
+  using V = typename cpx<T>::t;
+  V out[NS];
+  V in[IN_REGS ? NS : 1];
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+    out[a] = V{0, 0};
+    if (IN_REGS) in[a] = at(a);
+  }
+  int pidx = 0;
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+    const V ina = IN_REGS ? in[a] : at(a);
+#pragma unroll
+    for (int b = a; b < NS; ++b, ++pidx) {
+      const T v = Bs[pidx * npt + q];
+      const V inb = IN_REGS ? in[b] : at(b);
+      out[a].x += inb.x * v;
+      out[a].y += inb.y * v;
+      if (b != a) {
+        out[b].x += ina.x * v;
+        out[b].y += ina.y * v;
+      }
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < NS; ++a) at(a) = out[a];
+}
+
+// The same contraction with the closed form of Bmatrix (F:328-412) in FP32:
+// B_ab(k) = (E_ab - u_a . t_b) / mu with E_ab = eps_a : sigma_b, t_b = sigma_b f,
+// u_a = G(f) t_a, applied in factored form: with W = sum_b sigma_b S_b (a
+// symmetric tensor), w = W f and g = G w,
+//   sum_b B_ab S_b = (eps_a : W - sigma_a : sym(g f)) / mu,
+// 24 products per field instead of 2 NS per pair; k = 0 gives 0.  x: the
+// point's x index (N1 = L), c: its inner index j * N3 + k.
+template <int NS, typename At>
+__device__ __forceinline__ void contract_bfly(const BFlyParams &bf, At at, int x, int L, long long c) {
+  using V = float2;
+  const int j = (int)(c >> bf.lgN3), kz = (int)(c & (bf.n3 - 1));
+  const float f0 = frec_f(x, L, bf.d[0]), f1 = frec_f(j, bf.n2, bf.d[1]), f2 = frec_f(kz, bf.n3, bf.d[2]);
+  const float ff = f0 * f0 + f1 * f1 + f2 * f2;
+  if (!(ff > 0.0f)) {
+#pragma unroll
+    for (int a = 0; a < NS; ++a) at(a) = V{0, 0};
+    return;
+  }
+  V W[6];
+#pragma unroll
+  for (int cc = 0; cc < 6; ++cc) W[cc] = V{0, 0};
+#pragma unroll
+  for (int b = 0; b < NS; ++b) {
+    const V in = at(b);
+#pragma unroll
+    for (int cc = 0; cc < 6; ++cc) {
+      W[cc].x += bf.sig6[b][cc] * in.x;
+      W[cc].y += bf.sig6[b][cc] * in.y;
+    }
+  }
+  // G(f) (the inverse acoustic tensor over |f|^2, as in Bmatrix)
+  const float inv = 1.0f / ff;
+  const float z0 = f0 * f0 * inv, z1 = f1 * f1 * inv, z2 = f2 * f2 * inv;
+  const float d0 = bf.mu + bf.mup * z0, d1 = bf.mu + bf.mup * z1, d2 = bf.mu + bf.mup * z2;
+  const float i0 = 1.0f / d0, i1 = 1.0f / d1, i2 = 1.0f / d2;
+  const float kk = 1.0f + (bf.mu + bf.ll) * (i0 * z0 + i1 * z1 + i2 * z2);
+  const float cg = (bf.mu + bf.ll) / kk * inv;
+  const float G00 = inv * (i0 - f0 * f0 * i0 * i0 * cg);
+  const float G11 = inv * (i1 - f1 * f1 * i1 * i1 * cg);
+  const float G22 = inv * (i2 - f2 * f2 * i2 * i2 * cg);
+  const float G01 = -inv * f0 * f1 * i0 * i1 * cg;
+  const float G02 = -inv * f0 * f2 * i0 * i2 * cg;
+  const float G12 = -inv * f1 * f2 * i1 * i2 * cg;
+  // w = W f, g = G w
+  V w0, w1, w2, g0, g1, g2;
+  w0.x = W[0].x * f0 + W[3].x * f1 + W[4].x * f2;  w0.y = W[0].y * f0 + W[3].y * f1 + W[4].y * f2;
+  w1.x = W[3].x * f0 + W[1].x * f1 + W[5].x * f2;  w1.y = W[3].y * f0 + W[1].y * f1 + W[5].y * f2;
+  w2.x = W[4].x * f0 + W[5].x * f1 + W[2].x * f2;  w2.y = W[4].y * f0 + W[5].y * f1 + W[2].y * f2;
+  g0.x = G00 * w0.x + G01 * w1.x + G02 * w2.x;  g0.y = G00 * w0.y + G01 * w1.y + G02 * w2.y;
+  g1.x = G01 * w0.x + G11 * w1.x + G12 * w2.x;  g1.y = G01 * w0.y + G11 * w1.y + G12 * w2.y;
+  g2.x = G02 * w0.x + G12 * w1.x + G22 * w2.x;  g2.y = G02 * w0.y + G12 * w1.y + G22 * w2.y;
+  // H = sym(g f)
+  V H[6];
+  H[0].x = g0.x * f0;  H[0].y = g0.y * f0;
+  H[1].x = g1.x * f1;  H[1].y = g1.y * f1;
+  H[2].x = g2.x * f2;  H[2].y = g2.y * f2;
+  H[3].x = 0.5f * (g0.x * f1 + g1.x * f0);  H[3].y = 0.5f * (g0.y * f1 + g1.y * f0);
+  H[4].x = 0.5f * (g0.x * f2 + g2.x * f0);  H[4].y = 0.5f * (g0.y * f2 + g2.y * f0);
+  H[5].x = 0.5f * (g1.x * f2 + g2.x * f1);  H[5].y = 0.5f * (g1.y * f2 + g2.y * f1);
+  // partial unroll: the per-field constants then come through uniform
+  // registers (a full unroll spills at 80 registers a thread)
+#pragma unroll 4
+  for (int a = 0; a < NS; ++a) {
+    V o{0, 0};
+#pragma unroll
+    for (int cc = 0; cc < 6; ++cc) {
+      o.x += bf.pe6[a][cc] * W[cc].x + bf.qs6[a][cc] * H[cc].x;
+      o.y += bf.pe6[a][cc] * W[cc].y + bf.qs6[a][cc] * H[cc].y;
+    }
+    at(a) = o;
+  }
+}
+
 // Shared-memory bytes of the fused x-pass for a tile of T = 2^lgT.
 __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, int pitch, size_t vsize,
                                                         size_t bsize) {
@@ -432,11 +680,12 @@ __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, 
 // during the forward FFT.  One point per thread
 // in the contraction; IN_REGS keeps its NS inputs in registers (FP32, up to
 // 384 threads); FP64 reads them from shared memory and runs at most 256 threads.
-// BFLY (FP32 only): B_ab(k) = (E_ab - u_a . t_b) / mu with t_b = sigma_b f and
-// u_a = G(f) t_a, the closed form of Bmatrix (F:328-412), evaluated per point in
-// FP32 registers; no B table is read (the x-pass then moves only the fields).
+// BFLY (FP32 only): the contraction with the closed form of Bmatrix
+// (F:328-412) evaluated per point in FP32 registers, factored through the
+// symmetric tensor W = sum_b sigma_b S_b; no B table is read (the x-pass then
+// moves only the fields).
 template <typename T, int NS, bool IN_REGS, int LG, bool BFLY>
-__global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_kernel(XParams p) {
+__global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kernel(XParams p) {
   using V = typename cpx<T>::t;
   constexpr int P = NS * (NS + 1) / 2;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -494,73 +743,9 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   __syncthreads();
   for (int q = tid; q < npt; q += nthr) {
     const int t = q >> lgL, x = q & (L - 1);
-    V out[NS];
-    V in[IN_REGS ? NS : 1];
-#pragma unroll
-    for (int a = 0; a < NS; ++a) {
-      out[a] = V{0, 0};
-      if (IN_REGS) in[a] = sm[sidx(a, t, x)];
-    }
-    // closed-form B(k) of this point (BFLY): frequencies, G(f), t_b = sigma_b f
-    float G00 = 0, G01 = 0, G02 = 0, G11 = 0, G12 = 0, G22 = 0, tv[BFLY ? NS : 1][3];
-    bool nonzero = true;
-    if (BFLY) {
-      const BFlyParams &bf = p.bf;
-      const long long c = c0 + t;
-      const int j = (int)(c >> bf.lgN3), k = (int)(c & (bf.n3 - 1));
-      const float f0 = frec_f(x, L, bf.d[0]), f1 = frec_f(j, bf.n2, bf.d[1]), f2 = frec_f(k, bf.n3, bf.d[2]);
-      const float ff = f0 * f0 + f1 * f1 + f2 * f2;
-      nonzero = ff > 0.0f;
-      if (nonzero) {
-        const float inv = 1.0f / ff;
-        const float z0 = f0 * f0 * inv, z1 = f1 * f1 * inv, z2 = f2 * f2 * inv;
-        const float d0 = bf.mu + bf.mup * z0, d1 = bf.mu + bf.mup * z1, d2 = bf.mu + bf.mup * z2;
-        const float i0 = 1.0f / d0, i1 = 1.0f / d1, i2 = 1.0f / d2;
-        const float kk = 1.0f + (bf.mu + bf.ll) * (i0 * z0 + i1 * z1 + i2 * z2);
-        const float cc = (bf.mu + bf.ll) / kk * inv;
-        G00 = inv * (i0 - f0 * f0 * i0 * i0 * cc);
-        G11 = inv * (i1 - f1 * f1 * i1 * i1 * cc);
-        G22 = inv * (i2 - f2 * f2 * i2 * i2 * cc);
-        G01 = -inv * f0 * f1 * i0 * i1 * cc;
-        G02 = -inv * f0 * f2 * i0 * i2 * cc;
-        G12 = -inv * f1 * f2 * i1 * i2 * cc;
-#pragma unroll
-        for (int b = 0; b < (BFLY ? NS : 1); ++b)
-#pragma unroll
-          for (int i = 0; i < 3; ++i) tv[b][i] = bf.sig[b][i][0] * f0 + bf.sig[b][i][1] * f1 + bf.sig[b][i][2] * f2;
-      }
-    }
-    int pidx = 0;
-#pragma unroll
-    for (int a = 0; a < NS; ++a) {
-      const V ina = IN_REGS ? in[a] : sm[sidx(a, t, x)];
-      float ua0 = 0, ua1 = 0, ua2 = 0;
-      if (BFLY) {
-        const int aa = BFLY ? a : 0;
-        ua0 = G00 * tv[aa][0] + G01 * tv[aa][1] + G02 * tv[aa][2];
-        ua1 = G01 * tv[aa][0] + G11 * tv[aa][1] + G12 * tv[aa][2];
-        ua2 = G02 * tv[aa][0] + G12 * tv[aa][1] + G22 * tv[aa][2];
-      }
-#pragma unroll
-      for (int b = a; b < NS; ++b, ++pidx) {
-        T v;
-        if (BFLY) {
-          const int bb = BFLY ? b : 0;
-          v = nonzero ? (p.bf.E[pidx] - (ua0 * tv[bb][0] + ua1 * tv[bb][1] + ua2 * tv[bb][2])) * p.bf.mu_inv : (T)0;
-        } else {
-          v = Bs[pidx * npt + q];
-        }
-        const V inb = IN_REGS ? in[b] : sm[sidx(b, t, x)];
-        out[a].x += inb.x * v;
-        out[a].y += inb.y * v;
-        if (b != a) {
-          out[b].x += ina.x * v;
-          out[b].y += ina.y * v;
-        }
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < NS; ++a) sm[sidx(a, t, x)] = out[a];
+    auto at = [&](int a) -> V & { return sm[sidx(a, t, x)]; };
+    if constexpr (BFLY) contract_bfly<NS>(p.bf, at, x, L, c0 + t);
+    else contract_table<T, NS, IN_REGS>(Bs, npt, q, at);
   }
   __syncthreads();
   for (int l0 = 0; l0 < lines; l0 += teams) {
@@ -571,6 +756,98 @@ __global__ void __launch_bounds__((IN_REGS && !BFLY) ? 384 : 256, 2) x_fused_ker
   for (int e = tid; e < nel; e += nthr) {
     const int x = e & (L - 1), ln = e >> lgL;
     Sr[goff(ln) + x] = sm[ln * LP + x];
+  }
+}
+
+// Line pitch and swizzle of the warp-team x-pass (FP32 spectra, 8-byte
+// elements): element l of a tile line sits at line * xw_pitch(L) + (l ^ ((l >>
+// lgNV) & (LV - 1))) with LV = L / NV lanes per line.  The pitch puts the
+// 16 / LV lines of one 128-byte shared-memory phase side by side and the XOR
+// spreads a stage's strided writes, so no FFT stage and no contraction access
+// has a bank conflict (checked for N1 = 32..256 by the host tests).
+__host__ __device__ constexpr int xw_lv(int lgL) { return (1 << lgL) / xpass_nv(lgL, 8); }
+__host__ __device__ constexpr int xw_pitch(int lgL) { return (1 << lgL) + (xw_lv(lgL) < 16 ? xw_lv(lgL) : 16); }
+__host__ __device__ __forceinline__ int xw_swz(int l, int lgL) {
+  const int lgNV = xpass_nv(lgL, 8) == 16 ? 4 : 3;
+  return l ^ ((l >> lgNV) & (xw_lv(lgL) - 1));
+}
+
+// Shared-memory bytes of the warp-team x-pass: twiddles | tile lines |
+// B tile (bsize 0: B evaluated in registers).
+__host__ __device__ __forceinline__ size_t xw_smem(int ns, int lgL, int lgT, size_t bsize) {
+  const size_t head = (((size_t)1 << lgL) + (size_t)ns * ((size_t)1 << lgT) * xw_pitch(lgL)) * 8;
+  const size_t P = (size_t)ns * (ns + 1) / 2;
+  return ((head + 15) & ~(size_t)15) + P * ((size_t)1 << (lgL + lgT)) * bsize;
+}
+
+// Fused x-pass with warp-resident line teams (FP32 spectra, N1 = 32..256):
+// the same transform, contraction and results as x_fused_kernel, laid out so
+// that each line's L/NV threads are lanes of one warp.  A line goes straight
+// from global memory into registers (lanes on consecutive x), through the
+// forward FFT's stages in the warp's own lines of shared memory (warp
+// barriers only), and back out of the inverse FFT's last stage straight to
+// global memory; the block synchronises only around the contraction, which
+// mixes the fields of a point.  The B tile (table form) streams in by TMA
+// bulk copies during the forward FFT.
+template <int NS, int LG, bool BFLY>
+__global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
+  using V = float2;
+  static_assert(LG >= 5 && LG <= 8, "the warp-team x-pass covers N1 = 32..256");
+  constexpr int L = 1 << LG, P = NS * (NS + 1) / 2;
+  constexpr int NV = xpass_nv(LG, 8), LV = L / NV, LPW = 32 / LV, LP = xw_pitch(LG);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lgT = p.lgT, TT = 1 << lgT, lines = NS << lgT, npt = L << lgT;
+  V *tws = reinterpret_cast<V *>(smraw);
+  V *sm = tws + L;
+  const size_t head = (((size_t)L + (size_t)lines * LP) * sizeof(V) + 15) & ~(size_t)15;
+  float *Bs = reinterpret_cast<float *>(smraw + head);
+  const long long r = blockIdx.x / p.tiles;
+  const long long tile = blockIdx.x - r * p.tiles;
+  if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
+  if (p.active && !p.active[r]) return;
+  const long long c0 = tile << lgT;
+  const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+  const int th = lane & (LV - 1), wl = lane / LV;  // team thread, line of the warp
+  V *Sr = reinterpret_cast<V *>(p.S) + ((long long)r * NS * p.inner + c0) * L;
+  const int fstride = (int)p.inner * L;
+  auto goff = [&](int ln) { return (ln >> lgT) * fstride + (ln & (TT - 1)) * L; };
+  __shared__ __align__(8) uint64_t bbar;
+  if (!BFLY && tid == 0) {  // B tile: P * npt contiguous values (a multiple of 16 bytes)
+    mbar_init(&bbar, 1);
+    bulk_load(Bs, reinterpret_cast<const float *>(p.B) + tile * P * (long long)npt, (unsigned)(P * npt * 4), &bbar);
+  }
+  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  __syncthreads();  // twiddles (the second stage on) and the barrier's initialisation
+  for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
+    const int ln = ln0 + wl;
+    const bool act = ln < lines;
+    V *line = sm + ln * LP;
+    V v[NV];
+    if (act) {
+      const V *g = Sr + goff(ln) + th;
+#pragma unroll
+      for (int m = 0; m < NV; ++m) v[m] = g[m * LV];
+    }
+    line_fft_io<-1, LG, true, false, NV, true>(v, th, tws, [&](int l) { return &line[xw_swz(l, LG)]; },
+                                               [&](int l) { return &line[xw_swz(l, LG)]; }, act);
+  }
+  if (!BFLY) mbar_wait(&bbar, 0, p.err);
+  __syncthreads();
+  for (int q = tid; q < npt; q += nthr) {
+    const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
+    auto at = [&](int a) -> V & { return sm[(a * TT + t) * LP + sx]; };
+    if constexpr (BFLY) contract_bfly<NS>(p.bf, at, x, L, c0 + t);
+    else contract_table<float, NS, true>(Bs, npt, q, at);
+  }
+  __syncthreads();
+  for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
+    const int ln = ln0 + wl;
+    const bool act = ln < lines;
+    V *line = sm + ln * LP;
+    V *g = Sr + (act ? goff(ln) : 0);
+    V v[NV];
+    line_fft_io<+1, LG, false, true, NV, true>(v, th, tws, [&](int l) { return &line[xw_swz(l, LG)]; },
+                                               [&](int l) { return &g[l]; }, act);
   }
 }
 

@@ -15,6 +15,10 @@ namespace pfdd {
 // z-pass for lgL in [0, 9]; prec 0 = FP64 spectra, 1 = FP32
 cudaError_t launch_zpass(int prec, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                          const ZParams &p);
+// pipelined z-pass of the FP32-FFT form (x-fastest S, full step) for lgL in
+// [3, 9]: `grid` persistent CTAs over `ntiles` tiles
+cudaError_t launch_zpass_pipe(int lgL, unsigned grid, int threads, size_t smem, cudaStream_t st, const ZParams &p,
+                              int ntiles);
 // strided line FFT (sign -1 forward, +1 inverse) for lgL in [0, 9]
 cudaError_t launch_strided(int prec, int sign, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                            void *data, int lgTI, long long inner, long long tiles_per_outer, const void *tw,
@@ -25,6 +29,9 @@ cudaError_t launch_x_fused_f64(int ns, unsigned blocks, int threads, size_t smem
 // FP32 x-pass evaluating B(k) in registers, N1 in [32, 256]
 cudaError_t launch_x_fused_f32_bfly(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                                     const XParams &p);
+// warp-team FP32 x-pass (stored or register-evaluated B(k)), N1 in [32, 256]
+cudaError_t launch_x_warp_f32(int ns, bool bfly, unsigned blocks, int threads, size_t smem, cudaStream_t st,
+                              const XParams &p);
 
 // Launch geometry of the z-pass, the strided passes and the fused x-pass for one
 // grid (ns = 0: FFT-boundary plans without the x-pass).  Sizes: powers of two <= 512.
@@ -57,16 +64,17 @@ struct Geometry {
   // spectral layout of a context's S: x fastest ([y][z][x] per field); the
   // FFT-boundary plans keep the natural [x][y][z]
   bool xfast = false;
-  // z-pass
-  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0;
-  size_t zSmem = 0;
+  // z-pass; zPipe > 0: the step's z-pass runs pipelined (zpass_pipe_kernel)
+  // with zPipe persistent CTAs per SM and zPipeSmem bytes each
+  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0, zPipe = 0;
+  size_t zSmem = 0, zPipeSmem = 0;
   // strided passes (y: axis 1, x: axis 0; x only in the FFT-boundary plans)
   int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1};
   long long tiles[2] = {1, 1};
   size_t smem[2] = {0, 0};
-  // fused x-pass
+  // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel)
   int xLgT = 0, xPitch = 1, xThreads = 256;
-  bool xWide = false;
+  bool xWide = false, xWarp = false;
   long long xTiles = 1;
   size_t xSmem = 0;
 };
@@ -89,6 +97,8 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   const long long lines = (long long)n1 * n2;
   if (TL < 1 || TL > lines || (g.xfast && TL > n1) || (long long)TL * team3 > kThreads) return false;
   g.zTL = TL;
+  g.zPipe = 0;  // the pipelined form is chosen per line count (set_z_pipe)
+  g.zPipeSmem = 0;
   g.zThreads = TL * team3;
   g.zPitch = z_line_pitch(L3, TL, vsize);
   g.zNparts = (int)(lines / TL);
@@ -96,6 +106,23 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
   g.lgL3 = ilog2(L3);
   return g.zSmem <= kMaxDynSmem;
+}
+
+// Pipelined z-pass (FP32 spectra, x-fastest S, N3 >= 8) for the current z
+// lines per tile with cps persistent CTAs per SM (0: the plain z-pass).  The
+// CTAs of one SM share its 228 KB of shared memory (1 KB of it reserved per CTA).
+inline bool set_z_pipe(Geometry &g, int n3, size_t vsize, int cps) {
+  if (cps == 0) {
+    g.zPipe = 0;
+    g.zPipeSmem = 0;
+    return true;
+  }
+  if (vsize != 8 || !g.xfast || n3 < 8 || cps < 1) return false;
+  const size_t smem = zpipe_smem(n3, g.zTL, g.zPitch, vsize);
+  if (smem > kMaxDynSmem || (size_t)cps * (smem + 2048) > 228 * 1024) return false;
+  g.zPipe = cps;
+  g.zPipeSmem = smem;
+  return true;
 }
 
 // Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.
@@ -118,15 +145,33 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
 // stage touches as many different lines as it has lanes (no bank conflicts),
 // at the price of idle threads when the tile has fewer lines.
 inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT,
-                           bool wide = false) {
+                           bool wide = false, bool warp = false) {
   const long long innerx = (long long)n2 * n3;
   if ((1LL << lgT) > innerx) return false;
+  if (warp) {  // FP32 spectra, N1 = 32..256; a thread a point, at most 384
+    const int lgL = ilog2(n1);
+    if (wide || vsize != 8 || n1 < 32 || n1 > 256) return false;
+    const size_t smem = xw_smem(ns, lgL, lgT, bsize);
+    if (smem > kMaxDynSmem) return false;
+    const int lpw = 32 / xw_lv(lgL), lines = ns << lgT;
+    int thr = std::max(n1 << lgT, (lines + lpw - 1) / lpw * 32);
+    thr = std::min(384, (thr + 31) / 32 * 32);
+    g.xPitch = xw_pitch(lgL);
+    g.xLgT = lgT;
+    g.xTiles = innerx >> lgT;
+    g.xSmem = smem;
+    g.xThreads = thr;
+    g.xWide = false;
+    g.xWarp = true;
+    return true;
+  }
+  g.xWarp = false;
   const int pitch = line_pitch(n1);
   const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize);
   if (smem > kMaxDynSmem) return false;
   const int team = x_line_team(n1, vsize), lines = ns << lgT, npt = n1 << lgT;
   const int unit = std::max(32, team);
-  const int cap = (vsize == sizeof(double2) || bsize == 0) ? 256 : 384;  // x_fused_kernel launch bounds
+  const int cap = vsize == sizeof(double2) ? 256 : 384;  // x_fused_kernel launch bounds
   if (unit > cap) return false;
   const int phase = (int)(128 / vsize);
   const int lines_eff = wide ? (lines + phase - 1) / phase * phase : lines;

@@ -278,7 +278,7 @@ class Solver:
     def plan(self) -> dict:
         """Launch plan (tile widths, threads, shared memory, radix plans, autotune timings)."""
         import json
-        buf = C.create_string_buffer(4096)
+        buf = C.create_string_buffer(16384)
         self._check(self.L.pfdd_get_plan(self.h, buf, len(buf)), "pfdd_get_plan")
         return json.loads(buf.value.decode())
 

@@ -43,7 +43,7 @@ static void y_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, s
 }
 static void x_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, size_t bs) {
   const int team = team_of(n1, 2, vs);
-  const int cap = (vs == 16 || bs == 0) ? 256 : 384;
+  const int cap = vs == 16 ? 256 : 384;
   CHECK(g.xTiles << g.xLgT == (long long)n2 * n3, "x tiles");
   CHECK(g.xThreads >= team && g.xThreads % team == 0 && g.xThreads <= cap, "x threads");
   CHECK(g.xSmem == x_fused_smem(ns, n1, g.xLgT, g.xPitch, vs, bs) && g.xSmem <= kMaxDynSmem, "x smem");
@@ -69,7 +69,16 @@ int main() {
         const int cap = (int)std::min<long long>((long long)n1 * n2, (long long)g.zNparts * 4);
         for (int lg = 0; lg <= 5; ++lg) {
           Geometry h = g;
-          if (set_z_geometry(h, n1, n2, n3, vs, 1 << lg) && h.zNparts <= cap) z_ok(h, n1, n2, n3, ns, vs, bs);
+          if (set_z_geometry(h, n1, n2, n3, vs, 1 << lg) && h.zNparts <= cap) {
+            z_ok(h, n1, n2, n3, ns, vs, bs);
+            for (int cps = 1; cps <= 4; ++cps) {  // pipelined form: its CTAs of one SM fit together
+              Geometry q = h;
+              if (!set_z_pipe(q, n3, vs, cps)) continue;
+              CHECK(vs == 8 && n3 >= 8 && q.zPipe == cps, "z pipe form");
+              CHECK(q.zPipeSmem == zpipe_smem(n3, q.zTL, q.zPitch, vs) && q.zPipeSmem <= kMaxDynSmem &&
+                    (size_t)cps * (q.zPipeSmem + 2048) <= 228 * 1024, "z pipe smem");
+            }
+          }
           for (bool wide : {false, true}) {
             h = g;
             if (set_x_geometry(h, n1, n2, n3, ns, vs, bs, lg, wide)) x_ok(h, n1, n2, n3, ns, vs, bs);

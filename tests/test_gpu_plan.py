@@ -70,3 +70,84 @@ def test_plan_is_tuned_once_per_shape(native_lib):
     assert (p2["z_pass"], p2["x_pass"], p2["y_pass"]) == (p1["z_pass"], p1["x_pass"], p1["y_pass"])
     np.testing.assert_array_equal(g1, g2)
     np.testing.assert_array_equal(x1, x2)
+
+
+def pinned(spec, precision, plan, nrep=1, prepare=None):
+    old = os.environ.get("PFDD_PLAN")
+    if plan is None:
+        os.environ.pop("PFDD_PLAN", None)
+        os.environ["PFDD_NO_TUNE"] = "1"
+    else:
+        os.environ["PFDD_PLAN"] = plan
+    try:
+        s = native.solver_for(spec, precision, nrep=nrep)
+    finally:
+        os.environ.pop("PFDD_NO_TUNE", None)
+        if old is None:
+            os.environ.pop("PFDD_PLAN", None)
+        else:
+            os.environ["PFDD_PLAN"] = old
+    x0, b0 = workloads.initial_state(spec)
+    tau = native.spec_tau(spec)
+    if nrep > 1:
+        s.set_state(np.stack([x0 * (1.0 - 0.3 * i) for i in range(nrep)]), np.stack([b0] * nrep))
+        tau = np.stack([tau] * nrep, axis=1)
+    else:
+        s.set_state(x0, b0)
+    if prepare:
+        prepare(s, b0)
+    g, ga = s.step(tau)
+    out = (g, s.get_state(), s.plan())
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("plan", ["z=8,p=3", "z=16,p=2", "z=32,p=1", "z=8,p=4"])
+def test_pipelined_zpass_gives_same_bits(native_lib, plan):
+    """The persistent, double-buffered z-pass computes every tile as the
+    one-CTA-per-tile z-pass does: same gamma and state bits.  (Line counts of
+    at least 8: the partial-sum buffer holds 4x the default plan's tiles.)"""
+    spec = workloads.SolveSpec(n=(32, 16, 64), ns=12, steps=10, sigma_max=0.05, noise_seed=31,
+                               loops=workloads.random_loops((32, 16, 64), 4, 2.0, 6.0, 12, seed=31))
+    g1, x1, p1 = pinned(spec, "fp32", plan)
+    g0, x0, p0 = pinned(spec, "fp32", None)
+    assert p1["z_pass"]["pipelined_ctas_per_sm"] == int(plan.split("p=")[1])
+    assert p0["z_pass"]["pipelined_ctas_per_sm"] == 0
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(x1, x0)
+
+
+def test_pipelined_zpass_batched_pinned_and_idle(native_lib):
+    """Pinned points (the per-point path of the update), an idle replica whose
+    tiles are skipped, and a line length of 128."""
+    spec = workloads.SolveSpec(n=(16, 8, 128), ns=3, steps=12, sigma_max=0.05, noise_seed=32,
+                               loops=workloads.random_loops((16, 8, 128), 3, 2.0, 5.0, 3, seed=32))
+
+    def prep(s, b0):
+        bc = np.zeros((3,) + b0.shape); bc[:, :, 0, 0, :] = 1.0
+        s.set_state(s.get_state(), bc)
+        s.set_active(1, False)
+
+    res = [pinned(spec, "fp32", plan, nrep=3, prepare=prep) for plan in ("z=8,p=3", None)]
+    live = [0, 2]
+    np.testing.assert_array_equal(res[0][0][:, live], res[1][0][:, live])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    assert res[0][2]["z_pass"]["pipelined_ctas_per_sm"] == 3
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp32_bfly"])
+@pytest.mark.parametrize("n1,plan", [(32, "x=1,w=1"), (64, "x=2,w=1"), (128, "x=1,w=1"), (128, "x=4,w=1"),
+                                     (256, "x=1,w=1")])
+def test_warp_team_xpass_gives_same_bits(native_lib, precision, n1, plan):
+    """The warp-team x-pass (lines straight between global memory and
+    registers, warp-local FFT stages, swizzled shared-memory lines) computes
+    the block-team x-pass's bits, with a stored B(k) and with B(k) in registers."""
+    n = (n1, 8, 16)
+    spec = workloads.SolveSpec(n=n, ns=12, steps=6, sigma_max=0.05, noise_seed=33,
+                               loops=workloads.random_loops(n, 3, 1.5, 3.0, 12, seed=33))
+    g1, x1, p1 = pinned(spec, precision, plan)
+    g0, x0, p0 = pinned(spec, precision, None)
+    assert p1["x_pass"]["warp_teams"] == 1 and p0["x_pass"]["warp_teams"] == 0
+    assert p1["x_pass"]["tile_columns"] == int(plan.split(",")[0][2:])
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(x1, x0)
