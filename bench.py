@@ -3,11 +3,13 @@
 
 Workload (default): the 128^3 x 12 FCC solve (8 seeded loops, sigma_xz ramp
 0 -> 0.05 mu over 1000 steps).  The headline `value` is the steps/s of the
-FP32-FFT form (complex64 FFTs + FP32 B(k) contraction, FP64 xi state and sums);
-the plain FP64 form runs on the same inputs beside it and the relative error of
-the FP32 form's average plastic strain against it is reported ("forms").
+FP32-FFT form (complex64 FFTs and B(k) contraction, FP64 xi state and sums)
+with B(k) evaluated from its closed form in the x-pass ("fp32_bfly"); the form
+with the stored FP32 B(k) table ("fp32") and the plain FP64 form run on the
+same inputs beside it, and the error of the FP32 forms' average plastic strain
+against the FP64 form is reported ("forms").
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form fp32_bfly|fp32]
 
 Under torchrun each rank runs its own independent solve (replicas only: the
 path has no data exchange); value = all ranks' steps / max-over-ranks time.
@@ -40,6 +42,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="fp32_bfly", choices=["fp32_bfly", "fp32"],
+                    help="the headline FP32-FFT form: B(k) from its closed form in registers, or the stored table")
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--ns", type=int, default=12)
     ap.add_argument("--fp64-steps", type=int, default=0, help="timed steps of the FP64 form (default: steps/4)")
@@ -158,7 +162,7 @@ def algorithmic_bytes(kernel: str, prec: str, n_pts: int, rf: int, ns: int) -> f
     if kernel.startswith("fft_"):
         return rf * n_pts * 2 * v
     if kernel in ("contract", "x_fused"):
-        return rf * n_pts * 2 * v + P * n_pts * b
+        return rf * n_pts * 2 * v + (0 if prec == "fp32_bfly" else P * n_pts * b)
     return 0.0
 
 
@@ -176,7 +180,10 @@ def profiled_traffic(kernel: str, prec: str, n: int, ns: int) -> float | None:
     if not p.exists():
         return None
     d = json.loads(p.read_text())
-    return d.get(f"{kernel}/{prec}/{n}^3x{ns}")
+    key = f"{kernel}/{prec}/{n}^3x{ns}"
+    if key not in d and prec == "fp32_bfly" and kernel != "x_fused":  # the FP32 forms share every other kernel
+        key = f"{kernel}/fp32/{n}^3x{ns}"
+    return d.get(key)
 
 
 def time_form(native, workloads, spec, prec, W, K, device, dist, clocks=None, profile=True):
@@ -295,10 +302,11 @@ def _class_step_ms(native, spec, xi, prec, dev, W=3, K=10):
     return e0.elapsed_time(e1) / K
 
 
-def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_steps=25):
+def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_steps=25, form="fp32_bfly"):
     """The 96-request uneven serving mix through the native server (pfdd_server_*),
-    FP32-FFT form: once with every request queued at t=0 (saturated throughput),
-    once with Poisson arrivals at `load` x that throughput (time-to-solution)."""
+    FP32-FFT form `form`: once with every request queued at t=0 (saturated
+    throughput), once with Poisson arrivals at `load` x that throughput
+    (time-to-solution)."""
     from pfdd_gb300 import serve
     reqs = workloads.config4_requests(scale_steps=scale)
     # one seeded initial state per (grid, systems) class, reused by the class's
@@ -323,15 +331,15 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     for key, xi in inputs.items():
         sp = next(r for r in reqs if (r.n, r.ns) == key)
         z = xi[..., 0] + 1j * xi[..., 1]
-        solo[key] = {p: _class_step_ms(native, sp, z, p, dev) for p in ("fp32", "fp64")}
+        solo[key] = {p: _class_step_ms(native, sp, z, p, dev) for p in (form, "fp64")}
     total_steps = sum(sp.steps for sp in reqs)
     total_updates = sum(sp.steps * sp.npts * sp.ns for sp in reqs)
-    seq = {p: sum(sp.steps * solo[(sp.n, sp.ns)][p] for sp in reqs) / 1e3 for p in ("fp32", "fp64")}
+    seq = {p: sum(sp.steps * solo[(sp.n, sp.ns)][p] for sp in reqs) / 1e3 for p in (form, "fp64")}
 
     trace = os.environ.get("PFDD_SERVER_TRACE_BASE")  # optional per-run scheduling traces
     if trace:
         os.environ["PFDD_SERVER_TRACE"] = trace + ".saturated.csv"
-    with serve.Server("fp32", device=dev, max_slots=max_slots, chunk_steps=chunk_steps) as srv:
+    with serve.Server(form, device=dev, max_slots=max_slots, chunk_steps=chunk_steps) as srv:
         t0 = time.perf_counter()
         ids = [submit(srv, sp) for sp in reqs]
         res = [srv.wait(i) for i in ids]
@@ -343,7 +351,7 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     arrive = np.cumsum(gaps) - gaps[0]
     if trace:
         os.environ["PFDD_SERVER_TRACE"] = trace + ".poisson.csv"
-    with serve.Server("fp32", device=dev, max_slots=max_slots, chunk_steps=chunk_steps) as srv:
+    with serve.Server(form, device=dev, max_slots=max_slots, chunk_steps=chunk_steps) as srv:
         t0 = time.perf_counter()
         ids = []
         for sp, ta in zip(reqs, arrive):
@@ -355,10 +363,10 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
         t_poi = time.perf_counter() - t0
         st_poi = srv.stats()
     lat = np.array([r.latency_s for r in res])
-    svc = np.array([sp.steps * solo[(sp.n, sp.ns)]["fp32"] / 1e3 for sp in reqs])
+    svc = np.array([sp.steps * solo[(sp.n, sp.ns)][form] / 1e3 for sp in reqs])
     return {
         "workload": f"96 requests, grids {{32,64,128,256}}^3 p={{.4,.3,.2,.1}}, NS in {{3,12}}, 1-8 loops, "
-                    f"sigma_max U(0.01,0.06), steps U(200,2000) x {scale}; FP32-FFT form",
+                    f"sigma_max U(0.01,0.06), steps U(200,2000) x {scale}; FP32-FFT form {form}", "form": form,
         "requests": len(reqs), "solve_steps": total_steps, "point_system_updates": total_updates,
         "server": {"max_slots": max_slots, "chunk_steps": chunk_steps, "hbm_budget": "90% of free"},
         "saturated": {"makespan_s": round(t_sat, 3), "steps_per_s": round(total_steps / t_sat, 1),
@@ -373,9 +381,9 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
                     "p50_slowdown": round(float(np.percentile(lat / svc, 50)), 3),
                     "p99_slowdown": round(float(np.percentile(lat / svc, 99)), 3),
                     "classes_created": st_poi["classes_created"], "peak_bytes": st_poi["peak_bytes"]},
-        "one_at_a_time": {"fp64_s": round(seq["fp64"], 3), "fp32_s": round(seq["fp32"], 3),
+        "one_at_a_time": {"fp64_s": round(seq["fp64"], 3), "fp32_s": round(seq[form], 3),
                           "fp64_steps_per_s": round(total_steps / seq["fp64"], 1),
-                          "fp32_steps_per_s": round(total_steps / seq["fp32"], 1),
+                          "fp32_steps_per_s": round(total_steps / seq[form], 1),
                           "how": "sum over requests of steps x the device step time of a lone solve of "
                                  "its class (3 warm-up + 10 timed steps per class and form)"},
         "speedup_vs_fp64_one_at_a_time": round(seq["fp64"] / t_sat, 2),
@@ -384,8 +392,8 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     }
 
 
-def precision_curve(native, workloads, spec, dev, every=100):
-    """Config 2's report: the FP32-FFT form against the plain FP64 form (which
+def precision_curve(native, workloads, spec, dev, every=100, form="fp32_bfly"):
+    """Config 2's report: the FP32-FFT form `form` against the plain FP64 form (which
     matches the reference's FP64 run) on the same inputs over the whole
     1000-step ramp, every `every` steps: max |dxi|, the largest |d gamma| so
     far, that over the largest |gamma| so far (the curve crosses zero, where a
@@ -393,16 +401,16 @@ def precision_curve(native, workloads, spec, dev, every=100):
     x0, b0 = workloads.initial_state(spec)
     tau = native.spec_tau(spec)
     ctx = {}
-    for prec in ("fp32", "fp64"):
+    for prec in (form, "fp64"):
         ctx[prec] = native.solver_for(spec, prec, device=dev)
         ctx[prec].set_state(x0, b0)
     out, worst, dmax, gmax = [], 0.0, 0.0, 0.0
     for s0 in range(0, spec.steps, every):
         g = {p: c.step(tau[s0:s0 + every])[0][:, 0] for p, c in ctx.items()}
-        d = np.abs(g["fp32"] - g["fp64"])
+        d = np.abs(g[form] - g["fp64"])
         worst = max(worst, float(np.max(d / np.abs(g["fp64"]))))
         dmax, gmax = max(dmax, float(d.max())), max(gmax, float(np.abs(g["fp64"]).max()))
-        dxi = float(np.max(np.abs(ctx["fp32"].get_state() - ctx["fp64"].get_state())))
+        dxi = float(np.max(np.abs(ctx[form].get_state() - ctx["fp64"].get_state())))
         out.append({"step": s0 + every, "max_dxi": dxi, "max_dgamma": dmax, "dgamma_over_max_gamma": dmax / gmax,
                     "gamma_pointwise_rel_err": worst, "gamma_fp64": float(g["fp64"][-1])})
     for c in ctx.values():
@@ -432,16 +440,17 @@ def time_strain(native, workloads, spec, dev, reps=3):
             "what": "strain and stress fields (FP64) of the 128^3 x 12 initial state incl. work-buffer setup"}
 
 
-def run_batched(native, workloads, dev, K, K64, W=3, count=16):
+def run_batched(native, workloads, dev, K, K64, W=3, count=16, form="fp32_bfly"):
     """Batched stress sweep: `count` replicas of the 128^3 x 12 solve in one
-    context sharing B(k) (FP32-FFT form), aggregate steps/s; each replica's
-    average plastic strain against the same replicas run in the FP64 form."""
+    context sharing B(k) (FP32-FFT form `form`), aggregate steps/s; each
+    replica's average plastic strain against the same replicas run in the FP64
+    form."""
     import torch
     specs = workloads.config3_replicas(count)
     xs = np.stack([workloads.initial_state(sp)[0] for sp in specs])
     tau = np.stack([native.spec_tau(sp) for sp in specs], axis=1)   # [1000, R, ns]
     out = {}
-    for prec, steps in (("fp32", K), ("fp64", K64)):
+    for prec, steps in ((form, K), ("fp64", K64)):
         s = native.solver_for(specs[0], prec, nrep=count, device=dev)
         s.set_state(xs)
         stream = torch.cuda.ExternalStream(s.stream, device=f"cuda:{dev}")
@@ -454,7 +463,7 @@ def run_batched(native, workloads, dev, K, K64, W=3, count=16):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         out[prec] = {"ms": ms, "gamma": np.concatenate([g_w, g_t]), "launches": s.launches, "plan": s.plan()}
-        if prec == "fp32":  # per-kernel device time of a few more batched steps
+        if prec == form:  # per-kernel device time of a few more batched steps
             s.kernel_timing(True)
             s.step(tau[W + steps:W + steps + 5])
             out[prec]["kernels"] = {nm: {"launches": c_, "avg_us": round(1e3 * t_ / c_, 1)}
@@ -462,19 +471,19 @@ def run_batched(native, workloads, dev, K, K64, W=3, count=16):
             s.kernel_timing(False)
         s.close()
     kk = W + K64
-    g32, g64 = out["fp32"]["gamma"][:kk], out["fp64"]["gamma"][:kk]
+    g32, g64 = out[form]["gamma"][:kk], out["fp64"]["gamma"][:kk]
     err = np.max(np.abs(g32 - g64) / np.abs(g64), axis=0)
     return {
         "workload": f"{count} replicas of 128^3 x 12 (config-1 loops, noise seeds 100..{99 + count}, sigma_max "
-                    f"0.005..0.08 mu over 1000 steps), one context sharing B(k); FP32-FFT form",
-        "replicas": count, "steps": K, "warmup": W,
-        "steps_per_s": round(count * K / (out["fp32"]["ms"] / 1e3), 2),
-        "ms_per_batched_step": round(out["fp32"]["ms"] / K, 4),
-        "updates_per_s": round(count * K / (out["fp32"]["ms"] / 1e3) * 128 ** 3 * 12, 1),
+                    f"0.005..0.08 mu over 1000 steps), one context sharing B(k); FP32-FFT form {form}",
+        "form": form, "replicas": count, "steps": K, "warmup": W,
+        "steps_per_s": round(count * K / (out[form]["ms"] / 1e3), 2),
+        "ms_per_batched_step": round(out[form]["ms"] / K, 4),
+        "updates_per_s": round(count * K / (out[form]["ms"] / 1e3) * 128 ** 3 * 12, 1),
         "fp64_steps_per_s": round(count * K64 / (out["fp64"]["ms"] / 1e3), 2),
         "strain_rel_err_vs_fp64": [float(v) for v in err], "strain_err_steps": kk,
-        "gpu_launches": int(out["fp32"]["launches"]), "kernels": out["fp32"]["kernels"],
-        "plan": out["fp32"]["plan"],
+        "gpu_launches": int(out[form]["launches"]), "kernels": out[form]["kernels"],
+        "plan": out[form]["plan"],
     }
 
 
@@ -487,13 +496,14 @@ def run_ours(a):
     dist.barrier()
     dev = dist.local
     torch.cuda.set_device(dev)
+    head, other = a.form, ("fp32" if a.form == "fp32_bfly" else "fp32_bfly")
     if a.batched_only:
         print(json.dumps({"batched": run_batched(native, workloads, dev, a.batched_steps,
-                                                 max(5, a.batched_steps // 8))}), flush=True)
+                                                 max(5, a.batched_steps // 8), form=head)}), flush=True)
         dist.close()
         return
     if a.serve_only:
-        print(json.dumps({"serving": run_serving(native, workloads, dev, a.serve_scale)}), flush=True)
+        print(json.dumps({"serving": run_serving(native, workloads, dev, a.serve_scale, form=head)}), flush=True)
         dist.close()
         return
     spec = workloads.config1(n=a.n) if dist.world == 1 else workloads.config1(noise_seed=100 + dist.rank, n=a.n)
@@ -502,23 +512,18 @@ def run_ours(a):
     W, K = max(3, a.warmup), a.steps
     K64 = a.fp64_steps or max(10, K // 4)
     clocks = Clocks(dev)
-    r32 = time_form(native, workloads, spec, "fp32", W, K, dev, dist, clocks=clocks)
-    rbf = time_form(native, workloads, spec, "fp32_bfly", W, K, dev, dist)
+    rh = time_form(native, workloads, spec, head, W, K, dev, dist, clocks=clocks)
+    ro = time_form(native, workloads, spec, other, W, K, dev, dist)
     r64 = time_form(native, workloads, spec, "fp64", W, K64, dev, dist)
-    ms32 = dist.max(r32["ms"])
-    msbf = dist.max(rbf["ms"])
-    vbf = aggregate(dist.world, K, msbf)
-    bf_err = float(np.max(np.abs(rbf["gamma"][:min(K, K64)] - r64["gamma"][:min(K, K64)]) /
-                          np.abs(r64["gamma"][:min(K, K64)])))
-    ms64 = dist.max(r64["ms"])
-    v32 = aggregate(dist.world, K, ms32)
-    v64 = aggregate(dist.world, K64, ms64)
+    msh, mso, ms64 = dist.max(rh["ms"]), dist.max(ro["ms"]), dist.max(r64["ms"])
+    vh, vo, v64 = aggregate(dist.world, K, msh), aggregate(dist.world, K, mso), aggregate(dist.world, K64, ms64)
     kk = min(K, K64)
-    g32, g64 = r32["gamma"][:kk], r64["gamma"][:kk]
-    strain_err = float(np.max(np.abs(g32 - g64) / np.abs(g64)))
+    g64 = r64["gamma"][:kk]
+    err_h = float(np.max(np.abs(rh["gamma"][:kk] - g64) / np.abs(g64)))
+    err_o = float(np.max(np.abs(ro["gamma"][:kk] - g64) / np.abs(g64)))
     e2e = None
     if not a.no_e2e:
-        e = time_e2e(native, workloads, spec, "fp32", K, dev)
+        e = time_e2e(native, workloads, spec, head, K, dev)
         ems = dist.max(e["ms"])
         e2e = {"value": aggregate(dist.world, K, ems), "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
                "d2h_bytes_per_step": e["d2h"],
@@ -526,7 +531,7 @@ def run_ours(a):
                        "+ pfdd_get_state (xi to pinned host)"}
     # roofline of the dominant kernel of the headline form
     peaks = load_peaks()
-    ks = r32["kstats"]
+    ks = rh["kstats"]
     roof = None
     kern = {}
     if ks:
@@ -535,13 +540,14 @@ def run_ours(a):
             kern[nm] = {"launches": cnt, "avg_us": 1e3 * tot / cnt}
         cnt, tot = ks[top]
         avg_s = tot / cnt / 1e3
-        ab = algorithmic_bytes(top, "fp32", spec.npts, spec.ns, spec.ns)
+        ab = algorithmic_bytes(top, head, spec.npts, spec.ns, spec.ns)
         ach = ab / avg_s / 1e9
-        tr = profiled_traffic(top, "fp32", a.n, spec.ns)
+        tr = profiled_traffic(top, head, a.n, spec.ns)
         roof = {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": tr, "algorithmic_bytes": ab,
                 "peak_src": peaks["src"] + " (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback"}
-    step_bytes = spec.npts * (spec.ns * 32 + spec.ns * (spec.ns + 1) // 2 * 4)
+    # compulsory bytes of a step: xi in and out (and the B(k) table when stored)
+    step_bytes = spec.npts * (spec.ns * 32 + (0 if head == "fp32_bfly" else spec.ns * (spec.ns + 1) // 2 * 4))
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline and r64["B"] is not None:
         cpu = cpu_baseline_port(spec, r64["B"])
@@ -549,42 +555,46 @@ def run_ours(a):
     if dist.world == 1:
         strain = time_strain(native, workloads, spec, dev)
         if not a.no_curve:
-            curve = {"config1_128c_ns12": precision_curve(native, workloads, spec, dev),
-                     "config0_32c_ns3": precision_curve(native, workloads, workloads.config0(), dev, every=50)}
+            curve = {"form": head,
+                     "config1_128c_ns12": precision_curve(native, workloads, spec, dev, form=head),
+                     "config0_32c_ns3": precision_curve(native, workloads, workloads.config0(), dev, every=50,
+                                                        form=head)}
     batched = None
     if dist.world == 1 and a.batched_steps > 0:
-        batched = run_batched(native, workloads, dev, a.batched_steps, max(5, a.batched_steps // 8))
+        batched = run_batched(native, workloads, dev, a.batched_steps, max(5, a.batched_steps // 8), form=head)
     serving = None
     if dist.world == 1 and a.serve_scale > 0:
-        serving = run_serving(native, workloads, dev, a.serve_scale)
-    launches_per_step = r32["launches"] / K
+        serving = run_serving(native, workloads, dev, a.serve_scale, form=head)
+    launches_per_step = rh["launches"] / K
+    what = {"fp32_bfly": "FP32-FFT form with B(k) evaluated in the x-pass from its closed form (no stored table)",
+            "fp32": "FP32-FFT form with the stored FP32 B(k) table"}
+
+    def form_entry(v, ms, err, r):
+        return {"steps_per_s": round(v, 2), "ms_per_step": round(ms / K, 4), "strain_rel_err_vs_fp64": err,
+                "kernels": {nm: {"launches": c_, "avg_us": 1e3 * t_ / c_} for nm, (c_, t_) in r["kstats"].items()},
+                "plan": r["plan"]}
     out = {
-        "metric": METRIC, "value": round(v32, 2), "unit": "steps/s", "n_gpus": dist.world, "steps": K, "warmup": W,
-        "ms_per_step": round(ms32 / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "metric": METRIC, "value": round(vh, 2), "unit": "steps/s", "n_gpus": dist.world, "steps": K, "warmup": W,
+        "ms_per_step": round(msh / K, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded loops + noise, numpy PCG64)",
         "config": {"workload": f"{a.n}^3 x {spec.ns} FCC slip systems, 8 seeded loops, sigma_xz ramp 0->0.05 mu "
-                               f"over 1000 steps; FP32-FFT form (complex64 FFT/contraction, FP64 xi state + sums)",
-                   "grid": [a.n] * 3, "ns": spec.ns, "solves_per_gpu": 1, "global_batch": dist.world,
-                   "parallelism": f"replicas x{dist.world}", "l2": "inputs larger than L2 (xi 403 MB + S 201 MB + "
-                                                                   "B 327 MB per step, L2 126 MB)"},
-        "updates_per_s": round(v32 * spec.npts * spec.ns, 1),
+                               f"over 1000 steps; {what[head]} (complex64 FFT/contraction, FP64 xi state + sums)",
+                   "form": head, "grid": [a.n] * 3, "ns": spec.ns, "solves_per_gpu": 1, "global_batch": dist.world,
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (xi 403 MB + S 201 MB per step"
+                         + ("" if head == "fp32_bfly" else " + B 327 MB") + ", L2 126 MB)"},
+        "updates_per_s": round(vh * spec.npts * spec.ns, 1),
         "hbm_roofline_step": {"algorithmic_bytes_per_step": step_bytes,
-                              "achieved_gbs": round(step_bytes * v32 / dist.world / 1e9, 1),
-                              "frac": round(step_bytes * v32 / dist.world / 1e9 / peaks["hbm_gbs"], 4)},
-        "forms": {"fp32": {"steps_per_s": round(v32, 2), "ms_per_step": round(ms32 / K, 4)},
+                              "achieved_gbs": round(step_bytes * vh / dist.world / 1e9, 1),
+                              "frac": round(step_bytes * vh / dist.world / 1e9 / peaks["hbm_gbs"], 4)},
+        "forms": {head: dict(form_entry(vh, msh, err_h, rh), what=what[head], headline=True),
+                  other: dict(form_entry(vo, mso, err_o, ro), what=what[other]),
                   "fp64": {"steps_per_s": round(v64, 2), "ms_per_step": round(ms64 / K64, 4), "steps": K64,
                            "dtype": "f64"},
-                  "fp32_bfly": {"steps_per_s": round(vbf, 2), "ms_per_step": round(msbf / K, 4),
-                                "strain_rel_err_vs_fp64": bf_err,
-                                "kernels": {nm: {"launches": c_, "avg_us": 1e3 * t_ / c_}
-                                            for nm, (c_, t_) in rbf["kstats"].items()},
-                                "what": "FP32-FFT form with B(k) evaluated in the x-pass from its closed form "
-                                        "(no stored table)"},
-                  "ratio_fp32_over_fp64": round(v32 / v64, 2),
-                  "strain_rel_err_fp32_vs_fp64": strain_err, "strain_err_steps": kk},
-        "kernels": kern, "plan": r32["plan"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": int(r32["launches"]), "launches_per_step": round(launches_per_step, 2),
-        "clocks": r32["clocks"], "strain_stress": strain, "fp32_vs_fp64_every_100_steps": curve,
+                  "ratio_fp32_over_fp64": round(vh / v64, 2), "strain_err_steps": kk},
+        "kernels": kern, "plan": rh["plan"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(rh["launches"]), "launches_per_step": round(launches_per_step, 2),
+        "clocks": rh["clocks"], "strain_stress": strain, "fp32_vs_fp64_every_100_steps": curve,
         "batched": batched, "serving": serving,
     }
     if dist.rank == 0:

@@ -320,7 +320,7 @@ struct KTiming {
 
 struct pfdd_ctx {
   int n[3] = {0, 0, 0};
-  int ns = 0, nrep = 0, prec = 0, dev = 0, nsm = 1;
+  int ns = 0, nrep = 0, prec = 0, dev = 0;
   long long N = 0;
   cudaStream_t st = nullptr;
   void *S = nullptr;
@@ -489,7 +489,6 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   c->ns = ns; c->nrep = nrep; c->prec = precision; c->dev = device;
   c->N = (long long)n1 * n2 * n3;
   CK(c, cudaSetDevice(device));
-  CK(c, cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision), /*xfast=*/true);
   if (!c->g.valid)
@@ -776,13 +775,7 @@ static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
   const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
   t_begin(c);
-  cudaError_t e;
-  if (c->g.zPipe > 0 && flags == (Z_INV | Z_UPDATE | Z_FWD | Z_STORE)) {
-    const long long grid = std::min<long long>(blocks, (long long)c->nsm * c->g.zPipe);
-    e = launch_zpass_pipe(c->g.lgL3, (unsigned)grid, c->g.zThreads, c->g.zPipeSmem, c->st, zp, (int)blocks);
-  } else {
-    e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp);
-  }
+  cudaError_t e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp);
   t_end(c, (flags & Z_UPDATE) ? K_Z_STEP : K_Z_PROLOGUE);
   return e;
 }
@@ -863,10 +856,10 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   snprintf(b, sizeof b,
            "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld, \"warp_teams\": %d}, "
            "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
-           "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu, \"pipelined_ctas_per_sm\": %d}, "
+           "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
            "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": ",
            1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp, 1 << g.lgTI[0], g.threads[0], g.smem[0],
-           g.tiles[0], g.zTL, g.zThreads, g.zPipe ? g.zPipeSmem : g.zSmem, g.zPipe, radix_plan(c->n[0], xnv).c_str(),
+           g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
            radix_plan(c->n[1], fft_nv(ilog2(c->n[1]))).c_str(), radix_plan(c->n[2], zpass_nv(ilog2(c->n[2]), vs)).c_str(),
            kGraphSteps);
   return std::string(b) + tuning + "}";
@@ -876,7 +869,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
 // times each shape once; later contexts of the shape (serving classes, batch
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
-  int zTL, zPipe, xLgT, yLgTI;
+  int zTL, xLgT, yLgTI;
   bool xWide, xWarp;
   std::string timings;
 };
@@ -897,11 +890,10 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,p=<CTAs per SM>,x=<tile columns>,w=<0|1>,y=<tile columns>"
-  // pins the plan (each entry optional, ignored when it does not fit; p, the
-  // pipelined z-pass, after z; w=1, the warp-team x-pass, after x) instead of
-  // timing it, e.g. to profile the plan a timed run chose (a profiler distorts
-  // the timings)
+  // PFDD_PLAN="z=<lines>,x=<tile columns>,w=<0|1>,y=<tile columns>" pins the
+  // plan (each entry optional, ignored when it does not fit; w=1, the
+  // warp-team x-pass, after x) instead of timing it, e.g. to profile the plan a
+  // timed run chose (a profiler distorts the timings)
   if (const char *pin = std::getenv("PFDD_PLAN")) {
     const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
     for (const char *q = pin; *q;) {
@@ -910,7 +902,6 @@ static pfdd_status autotune(pfdd_ctx *c) {
       if (std::sscanf(q, "%c=%d", &key, &v) == 2 && v > 0) {
         Geometry g = c->g;
         const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v) && g.zNparts <= c->zparts_cap
-                        : key == 'p' ? set_z_pipe(g, c->n[2], vs, v)
                         : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v))
                         : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false, v == 1)
                         : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs)
@@ -934,7 +925,6 @@ static pfdd_status autotune(pfdd_ctx *c) {
       if (it != g_plans.end()) {
         Geometry g = c->g;
         if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
-            set_z_pipe(g, c->n[2], vs, it->second.zPipe) &&
             set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide,
                            it->second.xWarp) &&
             (c->n[1] == 1 ||
@@ -980,13 +970,9 @@ static pfdd_status autotune(pfdd_ctx *c) {
     fill_u64_kernel<<<1216, kThreads, 0, c->st>>>(reinterpret_cast<unsigned long long *>(c->xi),
                                                   (long long)c->ns * c->N * 2, 0x3fe0000000000000ull);
     cudaMemsetAsync(c->tau, 0, (size_t)c->nrep * c->ns * sizeof(double), c->st);
-    // each line count plain and pipelined with 2..4 persistent CTAs per SM
-    // (key "<lines>p<CTAs per SM>"); both compute every tile identically
-    for (int cand = 0; cand <= 6 * 4 - 1; ++cand) {
-      const int lgTL = cand >> 2, cps = (cand & 3) == 0 ? 0 : (cand & 3) + 1;
+    for (int lgTL = 0; lgTL <= 5; ++lgTL) {
       Geometry g = c->g;
       if (!set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, 1 << lgTL) || g.zNparts > c->zparts_cap) continue;
-      if (!set_z_pipe(g, c->n[2], vs, cps)) continue;
       c->g = g;
       ZParams zp = make_zparams(c);
       zp.step_ctr = nullptr;
@@ -994,10 +980,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
       const double us = time_us([&] { return ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
-      if (cps)
-        snprintf(b, sizeof b, "%s\"%dp%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, cps, us);
-      else
-        snprintf(b, sizeof b, "%s\"%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, us);
+      snprintf(b, sizeof b, "%s\"%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, us);
       zs += b;
     }
     c->g = best;
@@ -1045,7 +1028,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
              ys + "}}";
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      g_plans[key] = TunedPlan{c->g.zTL, c->g.zPipe, c->g.xLgT, c->g.lgTI[0], c->g.xWide, c->g.xWarp, tuning};
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.xWide, c->g.xWarp, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }

@@ -36,29 +36,6 @@ cudaError_t launch_zpass(int prec, int lgL, unsigned blocks, int threads, size_t
                    : zpass_t<float>(lgL, blocks, threads, smem, st, p);
 }
 
-template <int LG>
-static cudaError_t zpipe_lg(unsigned grid, int threads, size_t smem, cudaStream_t st, const ZParams &p, int ntiles) {
-  static SmemOptIn configured;
-  cudaError_t e = ensure_smem(zpass_pipe_kernel<LG>, smem, configured);
-  if (e != cudaSuccess) return e;
-  zpass_pipe_kernel<LG><<<grid, threads, smem, st>>>(p, ntiles);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_zpass_pipe(int lgL, unsigned grid, int threads, size_t smem, cudaStream_t st, const ZParams &p,
-                              int ntiles) {
-  switch (lgL) {
-    case 3: return zpipe_lg<3>(grid, threads, smem, st, p, ntiles);
-    case 4: return zpipe_lg<4>(grid, threads, smem, st, p, ntiles);
-    case 5: return zpipe_lg<5>(grid, threads, smem, st, p, ntiles);
-    case 6: return zpipe_lg<6>(grid, threads, smem, st, p, ntiles);
-    case 7: return zpipe_lg<7>(grid, threads, smem, st, p, ntiles);
-    case 8: return zpipe_lg<8>(grid, threads, smem, st, p, ntiles);
-    case 9: return zpipe_lg<9>(grid, threads, smem, st, p, ntiles);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
 struct StridedArgs {
   void *data;
   int lgTI;

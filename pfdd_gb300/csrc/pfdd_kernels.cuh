@@ -333,130 +333,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
   }
 }
 
-// Shared-memory bytes of the pipelined z-pass: twiddles | two S tiles [TL][P]
-// (16-byte aligned) | two FP64 state tiles [TL][L].
-__host__ __device__ __forceinline__ size_t zpipe_smem(int L, int TL, int P, size_t vsize) {
-  return ((((size_t)L + 2 * (size_t)TL * P) * vsize + 15) & ~(size_t)15) + 2 * (size_t)TL * L * 16;
-}
-
-// Pipelined z-pass of the FP32-FFT form for the step's x-fastest S: inverse
-// z-FFT, Euler update with gamma partials, forward z-FFT, for tiles of TL
-// lines (x0..x0+TL-1, y) of one field, exactly as zpass_kernel's block `tile`
-// computes them (same instructions per line and point, same partial slot).
-// Persistent CTAs take tiles blockIdx.x, + gridDim.x, ...; while one tile is
-// transformed and updated, the S values (cp.async, TL-element runs) and FP64
-// state lines (TMA bulk copies) of the CTA's next tile stream into the other
-// half of a double buffer, so the loads of every tile but the first overlap
-// compute.  Tiles of idle replicas are skipped.
-template <int LG>
-__global__ void __launch_bounds__(256, 2) zpass_pipe_kernel(ZParams p, int ntiles) {
-  using V = float2;
-  static_assert(LG >= 3, "the pipelined z-pass needs L >= 8");
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ long long red[32];
-  __shared__ __align__(8) uint64_t xbar[2];  // completion of the FP64 state tiles
-  constexpr int L = 1 << LG, NV = zpass_nv(LG, (int)sizeof(V)), team = L / NV;
-  const int TL = p.TL, P = p.pitch, lgTL = p.lgTL;
-  const int nel = TL << LG, tid = threadIdx.x, nthr = blockDim.x;
-  V *tws = reinterpret_cast<V *>(smraw);
-  V *sbuf = tws + L;  // [2][TL][P]
-  double2 *xbuf = reinterpret_cast<double2 *>(smraw + ((((size_t)L + 2 * (size_t)TL * P) * sizeof(V) + 15) &
-                                                       ~(size_t)15));  // [2][TL * L]
-  const int xblocks = p.n1 >> lgTL;
-  const int ls = p.n2 * L;  // xi stride between the tile's lines
-  const int step = p.step_ctr ? *p.step_ctr : p.step;
-  // tile -> field rf = r*ns + a, xi offset lb of its first line, S offset sb
-  struct Tile {
-    long long rf;
-    int lb, sb, part;
-  };
-  auto tile_of = [&](int tile) {
-    const long long line0 = (long long)tile * TL;
-    Tile q;
-    q.rf = line0 / p.lines_per_field;
-    const int lf0 = (int)(line0 - q.rf * p.lines_per_field);
-    const int bf = lf0 >> lgTL, x0 = (bf % xblocks) << lgTL, yj = bf / xblocks;
-    q.lb = (x0 * p.n2 + yj) * L;
-    q.sb = yj * L * p.n1 + x0;
-    q.part = lf0 >> lgTL;
-    return q;
-  };
-  auto live = [&](int tile) {
-    if (!p.active) return true;
-    const long long rf = (long long)tile * TL / p.lines_per_field;
-    return p.active[rf / p.ns] != 0;
-  };
-  auto next_live = [&](int tile) {
-    while (tile < ntiles && !live(tile)) tile += gridDim.x;
-    return tile;
-  };
-  // loads of a tile into buffer b: S by cp.async (consecutive lanes on
-  // consecutive x), the FP64 lines by one thread's bulk copies
-  auto issue = [&](int tile, int b) {
-    const Tile q = tile_of(tile);
-    V *Sb = sbuf + b * TL * P;
-    const V *Sf = reinterpret_cast<const V *>(p.S) + q.rf * p.N;
-    for (int e = tid; e < nel; e += nthr) {
-      const int t = e & (TL - 1), z = e >> lgTL;
-      cp_async_elem(&Sb[t * P + z], &Sf[q.sb + t + z * p.n1]);
-    }
-    cp_async_commit();
-    if (tid == 0) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive_expect_tx(&xbar[b], (unsigned)nel * 16u);
-      const double2 *xif = p.xi + q.rf * p.N;
-      for (int t = 0; t < TL; ++t) bulk_copy(xbuf + b * nel + (t << LG), xif + q.lb + t * ls, (unsigned)L * 16u, &xbar[b]);
-    }
-  };
-  if (tid == 0) {
-    mbar_init(&xbar[0], 1);
-    mbar_init(&xbar[1], 1);
-  }
-  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
-  __syncthreads();  // barriers initialised before any thread waits on them
-  const int t = tid & (TL - 1), th = tid >> lgTL;  // consecutive lanes on consecutive lines
-  const bool act = th < team;
-  int cur = next_live(blockIdx.x);
-  if (cur < ntiles) issue(cur, 0);
-  for (int it = 0; cur < ntiles; ++it) {
-    const int b = it & 1;
-    const int nxt = next_live(cur + gridDim.x);
-    // buffer b ^ 1 is free: every read of it (the previous tile's forward FFT
-    // and update) preceded a barrier this thread has passed
-    if (nxt < ntiles) {
-      issue(nxt, b ^ 1);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    __syncthreads();
-    const Tile q = tile_of(cur);
-    const int a = (int)(q.rf % p.ns), r = (int)(q.rf / p.ns);
-    V *sm = sbuf + b * TL * P;
-    V *Sf = reinterpret_cast<V *>(p.S) + q.rf * p.N;
-    auto line = [&](int l) { return &sm[t * P + l]; };
-    auto gline = [&](int l) { return &Sf[q.sb + t + l * p.n1]; };
-    line_fft<+1, LG, NV>(th, LG, tws, line, act);
-    mbar_wait(&xbar[b], (unsigned)(it >> 1) & 1u, p.err);
-    const UpdCoef<float> k(p, a);
-    const double tv = p.tau[((long long)step * p.R + r) * p.ns + a];
-    const float ctau0 = k.tau(tv);
-    bool big = false;
-    const ulonglong2 *xsb = reinterpret_cast<const ulonglong2 *>(xbuf + b * nel);
-    ulonglong2 *xg = reinterpret_cast<ulonglong2 *>(p.xi + q.rf * p.N);
-    const long long acc =
-        (p.bc || p.tau_field) ? update_tile_f32<true, LG>(p, k, ctau0, tv, a, q.rf * p.N, q.lb, ls, nel, P, sm, xsb, xg, big)
-                              : update_tile_f32<false, LG>(p, k, ctau0, tv, a, q.rf * p.N, q.lb, ls, nel, P, sm, xsb, xg, big);
-    const long long sum = block_sum_i64(acc, red);
-    const int anybig = __syncthreads_or(big);
-    if (tid == 0) p.part[((long long)step * p.R * p.ns + q.rf) * p.nparts + q.part] = anybig ? LLONG_MIN : sum;
-    __syncthreads();
-    V v[NV];
-    line_fft_io<-1, LG, false, true, NV>(v, th, tws, line, gline, act);  // last stage straight to S
-    cur = nxt;
-  }
-}
-
 // Batched line FFT along a strided axis: data viewed as [outer][L][inner],
 // one CTA transforms an L x TI tile (TI contiguous inner columns).
 // Shared memory: twiddles [L] | tile [L][pitch].

@@ -15,10 +15,6 @@ namespace pfdd {
 // z-pass for lgL in [0, 9]; prec 0 = FP64 spectra, 1 = FP32
 cudaError_t launch_zpass(int prec, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                          const ZParams &p);
-// pipelined z-pass of the FP32-FFT form (x-fastest S, full step) for lgL in
-// [3, 9]: `grid` persistent CTAs over `ntiles` tiles
-cudaError_t launch_zpass_pipe(int lgL, unsigned grid, int threads, size_t smem, cudaStream_t st, const ZParams &p,
-                              int ntiles);
 // strided line FFT (sign -1 forward, +1 inverse) for lgL in [0, 9]
 cudaError_t launch_strided(int prec, int sign, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                            void *data, int lgTI, long long inner, long long tiles_per_outer, const void *tw,
@@ -64,10 +60,9 @@ struct Geometry {
   // spectral layout of a context's S: x fastest ([y][z][x] per field); the
   // FFT-boundary plans keep the natural [x][y][z]
   bool xfast = false;
-  // z-pass; zPipe > 0: the step's z-pass runs pipelined (zpass_pipe_kernel)
-  // with zPipe persistent CTAs per SM and zPipeSmem bytes each
-  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0, zPipe = 0;
-  size_t zSmem = 0, zPipeSmem = 0;
+  // z-pass
+  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0;
+  size_t zSmem = 0;
   // strided passes (y: axis 1, x: axis 0; x only in the FFT-boundary plans)
   int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1};
   long long tiles[2] = {1, 1};
@@ -97,8 +92,6 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   const long long lines = (long long)n1 * n2;
   if (TL < 1 || TL > lines || (g.xfast && TL > n1) || (long long)TL * team3 > kThreads) return false;
   g.zTL = TL;
-  g.zPipe = 0;  // the pipelined form is chosen per line count (set_z_pipe)
-  g.zPipeSmem = 0;
   g.zThreads = TL * team3;
   g.zPitch = z_line_pitch(L3, TL, vsize);
   g.zNparts = (int)(lines / TL);
@@ -106,23 +99,6 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   g.zSmem = ((((size_t)L3 + (size_t)TL * g.zPitch) * vsize + 15) & ~(size_t)15) + (size_t)TL * L3 * 16;
   g.lgL3 = ilog2(L3);
   return g.zSmem <= kMaxDynSmem;
-}
-
-// Pipelined z-pass (FP32 spectra, x-fastest S, N3 >= 8) for the current z
-// lines per tile with cps persistent CTAs per SM (0: the plain z-pass).  The
-// CTAs of one SM share its 228 KB of shared memory (1 KB of it reserved per CTA).
-inline bool set_z_pipe(Geometry &g, int n3, size_t vsize, int cps) {
-  if (cps == 0) {
-    g.zPipe = 0;
-    g.zPipeSmem = 0;
-    return true;
-  }
-  if (vsize != 8 || !g.xfast || n3 < 8 || cps < 1) return false;
-  const size_t smem = zpipe_smem(n3, g.zTL, g.zPitch, vsize);
-  if (smem > kMaxDynSmem || (size_t)cps * (smem + 2048) > 228 * 1024) return false;
-  g.zPipe = cps;
-  g.zPipeSmem = smem;
-  return true;
 }
 
 // Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.

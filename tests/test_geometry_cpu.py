@@ -46,7 +46,8 @@ static void x_ok(const Geometry &g, int n1, int n2, int n3, int ns, size_t vs, s
   const int cap = vs == 16 ? 256 : 384;
   CHECK(g.xTiles << g.xLgT == (long long)n2 * n3, "x tiles");
   CHECK(g.xThreads >= team && g.xThreads % team == 0 && g.xThreads <= cap, "x threads");
-  CHECK(g.xSmem == x_fused_smem(ns, n1, g.xLgT, g.xPitch, vs, bs) && g.xSmem <= kMaxDynSmem, "x smem");
+  CHECK(g.xSmem == (g.xWarp ? xw_smem(ns, ilog2(n1), g.xLgT, bs) : x_fused_smem(ns, n1, g.xLgT, g.xPitch, vs, bs)) &&
+            g.xSmem <= kMaxDynSmem, "x smem");
 }
 int main() {
   const int sizes[][3] = {{8, 8, 8}, {16, 16, 16}, {32, 32, 32}, {64, 64, 64}, {128, 128, 128}, {256, 256, 256},
@@ -69,15 +70,13 @@ int main() {
         const int cap = (int)std::min<long long>((long long)n1 * n2, (long long)g.zNparts * 4);
         for (int lg = 0; lg <= 5; ++lg) {
           Geometry h = g;
-          if (set_z_geometry(h, n1, n2, n3, vs, 1 << lg) && h.zNparts <= cap) {
-            z_ok(h, n1, n2, n3, ns, vs, bs);
-            for (int cps = 1; cps <= 4; ++cps) {  // pipelined form: its CTAs of one SM fit together
-              Geometry q = h;
-              if (!set_z_pipe(q, n3, vs, cps)) continue;
-              CHECK(vs == 8 && n3 >= 8 && q.zPipe == cps, "z pipe form");
-              CHECK(q.zPipeSmem == zpipe_smem(n3, q.zTL, q.zPitch, vs) && q.zPipeSmem <= kMaxDynSmem &&
-                    (size_t)cps * (q.zPipeSmem + 2048) <= 228 * 1024, "z pipe smem");
-            }
+          if (set_z_geometry(h, n1, n2, n3, vs, 1 << lg) && h.zNparts <= cap) z_ok(h, n1, n2, n3, ns, vs, bs);
+          h = g;
+          if (set_x_geometry(h, n1, n2, n3, ns, vs, bs, lg, false, true)) {  // warp-team x-pass
+            x_ok(h, n1, n2, n3, ns, vs, bs);
+            CHECK(vs == 8 && n1 >= 32 && n1 <= 256 && h.xWarp, "x warp form");
+            CHECK(h.xSmem == xw_smem(ns, ilog2(n1), h.xLgT, bs) && h.xPitch == xw_pitch(ilog2(n1)) &&
+                  h.xThreads % 32 == 0, "x warp smem/pitch/threads");
           }
           for (bool wide : {false, true}) {
             h = g;

@@ -102,37 +102,23 @@ def pinned(spec, precision, plan, nrep=1, prepare=None):
     return out
 
 
-@pytest.mark.parametrize("plan", ["z=8,p=3", "z=16,p=2", "z=32,p=1", "z=8,p=4"])
-def test_pipelined_zpass_gives_same_bits(native_lib, plan):
-    """The persistent, double-buffered z-pass computes every tile as the
-    one-CTA-per-tile z-pass does: same gamma and state bits.  (Line counts of
-    at least 8: the partial-sum buffer holds 4x the default plan's tiles.)"""
-    spec = workloads.SolveSpec(n=(32, 16, 64), ns=12, steps=10, sigma_max=0.05, noise_seed=31,
-                               loops=workloads.random_loops((32, 16, 64), 4, 2.0, 6.0, 12, seed=31))
-    g1, x1, p1 = pinned(spec, "fp32", plan)
-    g0, x0, p0 = pinned(spec, "fp32", None)
-    assert p1["z_pass"]["pipelined_ctas_per_sm"] == int(plan.split("p=")[1])
-    assert p0["z_pass"]["pipelined_ctas_per_sm"] == 0
-    np.testing.assert_array_equal(g1, g0)
-    np.testing.assert_array_equal(x1, x0)
-
-
-def test_pipelined_zpass_batched_pinned_and_idle(native_lib):
-    """Pinned points (the per-point path of the update), an idle replica whose
-    tiles are skipped, and a line length of 128."""
-    spec = workloads.SolveSpec(n=(16, 8, 128), ns=3, steps=12, sigma_max=0.05, noise_seed=32,
-                               loops=workloads.random_loops((16, 8, 128), 3, 2.0, 5.0, 3, seed=32))
+@pytest.mark.parametrize("precision", ["fp32", "fp32_bfly"])
+def test_warp_team_xpass_batched_pinned_and_idle(native_lib, precision):
+    """The warp-team x-pass on a batch: an idle replica whose tiles are
+    skipped, pinned points, N1 = 128."""
+    spec = workloads.SolveSpec(n=(128, 8, 16), ns=3, steps=12, sigma_max=0.05, noise_seed=32,
+                               loops=workloads.random_loops((128, 8, 16), 3, 2.0, 5.0, 3, seed=32))
 
     def prep(s, b0):
         bc = np.zeros((3,) + b0.shape); bc[:, :, 0, 0, :] = 1.0
         s.set_state(s.get_state(), bc)
         s.set_active(1, False)
 
-    res = [pinned(spec, "fp32", plan, nrep=3, prepare=prep) for plan in ("z=8,p=3", None)]
+    res = [pinned(spec, precision, plan, nrep=3, prepare=prep) for plan in ("x=2,w=1", None)]
     live = [0, 2]
     np.testing.assert_array_equal(res[0][0][:, live], res[1][0][:, live])
     np.testing.assert_array_equal(res[0][1], res[1][1])
-    assert res[0][2]["z_pass"]["pipelined_ctas_per_sm"] == 3
+    assert res[0][2]["x_pass"]["warp_teams"] == 1
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp32_bfly"])
