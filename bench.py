@@ -3,13 +3,13 @@
 
 Workload (default): the 128^3 x 12 FCC solve (8 seeded loops, sigma_xz ramp
 0 -> 0.05 mu over 1000 steps).  The headline `value` is the steps/s of the
-FP32-FFT form (complex64 FFTs and B(k) contraction, FP64 xi state and sums)
-with B(k) evaluated from its closed form in the x-pass ("fp32_bfly"); the form
-with the stored FP32 B(k) table ("fp32") and the plain FP64 form run on the
-same inputs beside it, and the error of the FP32 forms' average plastic strain
-against the FP64 form is reported ("forms").
+FP32-FFT form (complex64 FFTs and B(k) contraction, B(k) built in FP64 and
+stored rounded to FP32, FP64 xi state and sums: "fp32"); the form that
+evaluates B(k) from its closed form in the x-pass ("fp32_bfly") and the plain
+FP64 form run on the same inputs beside it, and the error of the FP32 forms'
+average plastic strain against the FP64 form is reported ("forms").
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form fp32_bfly|fp32]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form fp32|fp32_bfly]
 
 Under torchrun each rank runs its own independent solve (replicas only: the
 path has no data exchange); value = all ranks' steps / max-over-ranks time.
@@ -42,8 +42,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp32_bfly", choices=["fp32_bfly", "fp32"],
-                    help="the headline FP32-FFT form: B(k) from its closed form in registers, or the stored table")
+    ap.add_argument("--form", default="fp32", choices=["fp32", "fp32_bfly"],
+                    help="the headline FP32-FFT form: the stored table (B(k) built in FP64, then rounded: the "
+                         "metric's form) or B(k) from its closed form in registers")
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--ns", type=int, default=12)
     ap.add_argument("--fp64-steps", type=int, default=0, help="timed steps of the FP64 form (default: steps/4)")
@@ -302,7 +303,7 @@ def _class_step_ms(native, spec, xi, prec, dev, W=3, K=10):
     return e0.elapsed_time(e1) / K
 
 
-def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_steps=25, form="fp32_bfly"):
+def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_steps=25, form="fp32"):
     """The 96-request uneven serving mix through the native server (pfdd_server_*),
     FP32-FFT form `form`: once with every request queued at t=0 (saturated
     throughput), once with Poisson arrivals at `load` x that throughput
@@ -392,7 +393,7 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     }
 
 
-def precision_curve(native, workloads, spec, dev, every=100, form="fp32_bfly"):
+def precision_curve(native, workloads, spec, dev, every=100, form="fp32"):
     """Config 2's report: the FP32-FFT form `form` against the plain FP64 form (which
     matches the reference's FP64 run) on the same inputs over the whole
     1000-step ramp, every `every` steps: max |dxi|, the largest |d gamma| so
@@ -440,7 +441,7 @@ def time_strain(native, workloads, spec, dev, reps=3):
             "what": "strain and stress fields (FP64) of the 128^3 x 12 initial state incl. work-buffer setup"}
 
 
-def run_batched(native, workloads, dev, K, K64, W=3, count=16, form="fp32_bfly"):
+def run_batched(native, workloads, dev, K, K64, W=3, count=16, form="fp32"):
     """Batched stress sweep: `count` replicas of the 128^3 x 12 solve in one
     context sharing B(k) (FP32-FFT form `form`), aggregate steps/s; each
     replica's average plastic strain against the same replicas run in the FP64
