@@ -197,6 +197,7 @@ __global__ void build_B_kernel(const BBuildParams *__restrict__ bp, BLayout bl, 
     if (!(f2 > 0)) {
       for (int q = 0; q < bl.P; ++q) {
         const long long bi = b_index(bl, q, pt);
+        if (bi < 0) continue;  // held by the mirrored point (tile table)
         if (Bd) Bd[bi] = 0.0;
         if (Bf) Bf[bi] = 0.0f;
       }
@@ -219,8 +220,9 @@ __global__ void build_B_kernel(const BBuildParams *__restrict__ bp, BLayout bl, 
     int q = 0;
     for (int a = 0; a < ns; ++a)
       for (int b = a; b < ns; ++b, ++q) {
-        const double v = (bp->E[a][b] - (t[a][0] * u[b][0] + t[a][1] * u[b][1] + t[a][2] * u[b][2])) * bp->mu_inv;
         const long long bi = b_index(bl, q, pt);
+        if (bi < 0) continue;
+        const double v = (bp->E[a][b] - (t[a][0] * u[b][0] + t[a][1] * u[b][1] + t[a][2] * u[b][2])) * bp->mu_inv;
         if (Bd) Bd[bi] = v;
         if (Bf) Bf[bi] = (float)v;
       }
@@ -235,8 +237,9 @@ __global__ void pack_B_kernel(const double *src, int ns, BLayout bl, double *Bd,
     int q = 0;
     for (int a = 0; a < ns; ++a)
       for (int b = a; b < ns; ++b, ++q) {
-        const double v = src[((long long)b * ns + a) * N + pt];
         const long long bi = b_index(bl, q, pt);
+        if (bi < 0) continue;  // the mirrored point's value (checked equal on the host)
+        const double v = src[((long long)b * ns + a) * N + pt];
         if (Bd) Bd[bi] = v;
         if (Bf) Bf[bi] = (float)v;
       }
@@ -251,7 +254,12 @@ __global__ void unpack_B_kernel(const double *Bd, const float *Bf, int ns, BLayo
     int q = 0;
     for (int a = 0; a < ns; ++a)
       for (int b = a; b < ns; ++b, ++q) {
-        const long long bi = b_index(bl, q, pt);
+        long long bi = b_index(bl, q, pt);
+        if (bi < 0) {  // a mirrored tile's second line: B at the point mirrored through the origin
+          const long long x = pt / bl.inner, cc = pt - x * bl.inner;
+          const int2 tp = bl.tiles[bl.line_tile[cc] >> 1];
+          bi = b_index(bl, q, (long long)b_mirror((int)x, bl.L) * bl.inner + tp.x);
+        }
         const double v = Bd ? Bd[bi] : (double)Bf[bi];
         dst[((long long)b * ns + a) * N + pt] = v;
         dst[((long long)a * ns + b) * N + pt] = v;
@@ -340,6 +348,13 @@ struct pfdd_ctx {
   int kchunk = 1;
   Geometry g;
   BLayout bl{};
+  // B(k) tile table of the FP32 stored-table form (see BLayout); xtSym: the
+  // mirrored layout (B(-k) = B(k)) is in use, else single tiles only
+  int2 *xt = nullptr;
+  long long *xtoff = nullptr;
+  int *xline = nullptr, *xord = nullptr;
+  long long ntiles = 0, bvals = 0;
+  bool xtSym = true;
   BFlyParams bf{};
   long long launches = 0;
   KTiming tm;
@@ -359,7 +374,7 @@ struct pfdd_ctx {
   std::vector<double> epsv;
   bool tuned = false, tune = true;
   int zparts_cap = 0;  // z-pass blocks per field the partial buffer holds
-  std::string plan;
+  std::string plan;  // the autotune record of the plan (JSON), reported with the current geometry
 };
 
 struct pfdd_fft_plan {
@@ -434,10 +449,21 @@ static size_t bsize_of(int prec) {
 }
 static bool prec_ok(int prec) { return prec == PFDD_FP64 || prec == PFDD_FFT_FP32 || prec == PFDD_FFT_FP32_BFLY; }
 
+// The FP32 stored-table form keeps B(k) in the tile-table layout.
+static bool uses_tile_table(int prec) { return prec == PFDD_FFT_FP32; }
+
+// B(k) values a context stores (the single-tile table is the largest layout)
+static size_t b_values(int n1, int n2, int n3, int ns, int prec) {
+  const size_t P = (size_t)ns * (ns + 1) / 2, N = (size_t)n1 * n2 * n3;
+  if (!uses_tile_table(prec)) return bsize_of(prec) ? P * N : 0;
+  return P * (size_t)n2 * n3 * (size_t)((n1 + 3) / 4 * 4);
+}
+
 extern "C" size_t pfdd_required_bytes(int n1, int n2, int n3, int ns, int nrep, int precision) {
   const size_t N = (size_t)n1 * n2 * n3, P = (size_t)ns * (ns + 1) / 2, RF = (size_t)nrep * ns;
   size_t b = RF * N * (sizeof(double2) + vsize_of(precision));  // xi + S
-  b += P * N * bsize_of(precision);                              // B
+  b += b_values(n1, n2, n3, ns, precision) * bsize_of(precision);  // B
+  (void)P;
   b += (RF * N + 31) / 32 * 4;                                   // bc mask
   b += 64u << 20;                                                // partials, tables, slack
   return b;
@@ -476,6 +502,38 @@ static cudaError_t make_twiddles(void **tw, const int n[3], int prec, cudaStream
 template <typename T>
 static pfdd_status autotune(pfdd_ctx *c);
 
+// Copies a tile table to the context's device arrays (sized for the single-
+// tile table, the largest) and records its tile count.
+static cudaError_t upload_tile_table(pfdd_ctx *c, const TileTable &t) {
+  cudaError_t e = cudaMemcpyAsync(c->xt, t.tiles.data(), t.tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->xtoff, t.toff.data(), t.toff.size() * sizeof(long long), cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->xline, t.line_tile.data(), t.line_tile.size() * sizeof(int), cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->xord, t.order.data(), t.order.size() * sizeof(int), cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);  // the host vectors go out of scope
+  c->ntiles = (long long)t.tiles.size();
+  return e;
+}
+
+// Switches the FP32 stored-table form between the mirrored tile table and the
+// single-tile one (a B(k) without the mirror symmetry); the x-pass grid changes
+// with it.
+static pfdd_status set_tile_layout(pfdd_ctx *c, bool symmetric) {
+  if (!uses_tile_table(c->prec) || c->xtSym == symmetric) return PFDD_OK;
+  const TileTable t = make_tile_table(c->n[0], c->n[1], c->n[2], c->ns * (c->ns + 1) / 2, symmetric);
+  CK(c, upload_tile_table(c, t));
+  c->xtSym = symmetric;
+  Geometry g = c->g;
+  if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vsize_of(c->prec), bsize_of(c->prec), g.xLgT, g.xWide,
+                      false, c->ntiles))
+    return fail(c, PFDD_EINVAL, "B(k) tile layout: the x-pass tile does not fit");
+  c->g = g;
+  c->gen++;  // captured x-pass launch shape
+  return PFDD_OK;
+}
+
 extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n3, int ns, int nrep, int precision,
                                            int device) {
   if (!out) return PFDD_EINVAL;
@@ -490,7 +548,12 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   c->N = (long long)n1 * n2 * n3;
   CK(c, cudaSetDevice(device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-  c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision), /*xfast=*/true);
+  TileTable tt;
+  if (uses_tile_table(precision)) {
+    tt = make_tile_table(n1, n2, n3, ns * (ns + 1) / 2, true);
+    c->ntiles = (long long)tt.tiles.size();
+  }
+  c->g = make_geometry(n1, n2, n3, ns, vsize_of(precision), bsize_of(precision), /*xfast=*/true, c->ntiles);
   if (!c->g.valid)
     return fail(c, PFDD_EINVAL,
                 "pfdd_create: one x-line tile of %d systems x N1=%d with its B(k) does not fit in shared memory in "
@@ -498,7 +561,16 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
   CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
   CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
-  if (bsize_of(precision)) CK(c, cudaMalloc(&c->B, P * N * bsize_of(precision)));
+  c->bvals = (long long)b_values(n1, n2, n3, ns, precision);
+  if (c->bvals) CK(c, cudaMalloc(&c->B, (size_t)c->bvals * bsize_of(precision)));
+  if (uses_tile_table(precision)) {
+    const size_t inner = (size_t)n2 * n3;
+    CK(c, cudaMalloc(&c->xt, inner * sizeof(int2)));
+    CK(c, cudaMalloc(&c->xtoff, (inner + 1) * sizeof(long long)));
+    CK(c, cudaMalloc(&c->xline, inner * sizeof(int)));
+    CK(c, cudaMalloc(&c->xord, inner * sizeof(int)));
+    CK(c, upload_tile_table(c, tt));
+  }
   CK(c, cudaMalloc(&c->active, nrep));
   CK(c, cudaMalloc(&c->dslip_dev, kMaxNs * sizeof(double)));
   CK(c, cudaMalloc(&c->flag, sizeof(int)));
@@ -526,12 +598,14 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   // tile widths are timed on the (zeroed) buffers before B(k) is laid out in
   // the chosen x-pass tile order
   CK(c, cudaMemsetAsync(c->S, 0, RF * N * vsize_of(precision), c->st));
-  if (c->B) CK(c, cudaMemsetAsync(c->B, 0, P * N * bsize_of(precision), c->st));
+  if (c->B) CK(c, cudaMemsetAsync(c->B, 0, (size_t)c->bvals * bsize_of(precision), c->st));
   {
     const pfdd_status st = precision == PFDD_FP64 ? autotune<double>(c) : autotune<float>(c);
     if (st != PFDD_OK) return st;
   }
-  c->bl = BLayout{c->N, (long long)n2 * n3, n1, c->g.xLgT, ns * (ns + 1) / 2};
+  c->bl = BLayout{c->N, (long long)n2 * n3, n1, c->g.xLgT, ns * (ns + 1) / 2, c->g.xTable ? c->xt : nullptr,
+                  c->g.xTable ? c->xtoff : nullptr, c->g.xTable ? c->xline : nullptr};
+  (void)P;
   CK(c, cudaStreamSynchronize(c->st));
   return PFDD_OK;
 }
@@ -547,7 +621,8 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   if (c->graph_many) cudaGraphExecDestroy(c->graph_many);
   if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
-                c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2]};
+                c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2],
+                c->xt, c->xtoff, c->xline, c->xord};
   if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
   for (void *p : dp)
@@ -564,6 +639,31 @@ extern "C" pfdd_status pfdd_set_B(pfdd_ctx *c, const double *B) {
   if (c->prec == PFDD_FFT_FP32_BFLY)
     return fail(c, PFDD_EINVAL, "pfdd_set_B: this context evaluates B(k) itself; use pfdd_build_B");
   CK(c, cudaSetDevice(c->dev));
+  if (uses_tile_table(c->prec)) {
+    // the mirrored tile layout holds one of each pair of points mirrored
+    // through the origin (see BLayout): use it only when the given B(k) has
+    // the same bits at both (a B(k) from the reference's formula does)
+    const int n1 = c->n[0], n2 = c->n[1], n3 = c->n[2], ns = c->ns;
+    const long long inner = (long long)n2 * n3, N = c->N;
+    bool sym = true;
+    for (long long cc = 0; cc < inner && sym; ++cc) {
+      const int j = (int)(cc / n3), k = (int)(cc % n3);
+      if (j == n2 / 2 || k == n3 / 2) continue;  // Nyquist lines are single tiles
+      const long long m = (long long)b_mirror(j, n2) * n3 + b_mirror(k, n3);
+      if (m <= cc) continue;
+      for (int x = 0; x < n1 && sym; ++x) {
+        if (x == n1 / 2) continue;  // stored for both lines
+        const long long p1 = (long long)x * inner + cc, p2 = (long long)b_mirror(x, n1) * inner + m;
+        for (int aa = 0; aa < ns && sym; ++aa)
+          for (int bb = aa; bb < ns; ++bb) {
+            const double *row = B + ((long long)bb * ns + aa) * N;
+            if (std::memcmp(row + p1, row + p2, sizeof(double)) != 0) { sym = false; break; }
+          }
+      }
+    }
+    const pfdd_status st = set_tile_layout(c, sym);
+    if (st != PFDD_OK) return st;
+  }
   const size_t full = (size_t)c->ns * c->ns * c->N * sizeof(double);
   double *tmp = nullptr;
   CK(c, cudaMalloc(&tmp, full));
@@ -653,6 +753,10 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
       }
     c->hasB = true;
     return PFDD_OK;
+  }
+  {
+    const pfdd_status st = set_tile_layout(c, true);  // the closed form has B(-k) = B(k) bit for bit
+    if (st != PFDD_OK) return st;
   }
   BBuildParams *dp = nullptr;
   CK(c, cudaMalloc(&dp, sizeof hp));
@@ -803,6 +907,10 @@ template <typename T>
 static cudaError_t launch_x_fused(pfdd_ctx *c) {
   XParams xp;
   xp.S = c->S; xp.B = c->B; xp.active = c->active; xp.tw = c->tw[0];
+  xp.xt = c->g.xTable ? c->xt : nullptr;
+  xp.xtoff = c->g.xTable ? c->xtoff : nullptr;
+  xp.xline = c->g.xTable ? c->xline : nullptr;
+  xp.xord = c->g.xTable ? c->xord : nullptr;
   xp.inner = (long long)c->n[1] * c->n[2]; xp.tiles = c->g.xTiles;
   xp.L = c->n[0]; xp.lgL = ilog2(c->n[0]); xp.lgT = c->g.xLgT; xp.pitch = c->g.xPitch; xp.R = c->nrep;
   xp.step_ctr = c->step_ctr;
@@ -854,11 +962,13 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   const int xnv = lgx >= 5 && lgx <= 8 ? xpass_nv(lgx, vs) : 8;  // the x-pass's compiled-in lengths
   char b[1024];  // the fixed part; the autotune timings follow
   snprintf(b, sizeof b,
-           "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld, \"warp_teams\": %d}, "
+           "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld, \"warp_teams\": %d, "
+           "\"b_tiles\": %lld, \"b_mirrored\": %d}, "
            "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
            "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
            "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": ",
-           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp, 1 << g.lgTI[0], g.threads[0], g.smem[0],
+           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp,
+           g.xTable ? c->ntiles : 0LL, (int)(g.xTable && c->xtSym), 1 << g.lgTI[0], g.threads[0], g.smem[0],
            g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
            radix_plan(c->n[1], fft_nv(ilog2(c->n[1]))).c_str(), radix_plan(c->n[2], zpass_nv(ilog2(c->n[2]), vs)).c_str(),
            kGraphSteps);
@@ -901,9 +1011,12 @@ static pfdd_status autotune(pfdd_ctx *c) {
       int v = 0;
       if (std::sscanf(q, "%c=%d", &key, &v) == 2 && v > 0) {
         Geometry g = c->g;
+        const long long tt = uses_tile_table(c->prec) ? c->ntiles : 0;
         const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v) && g.zNparts <= c->zparts_cap
-                        : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v))
-                        : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false, v == 1)
+                        : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v), false,
+                                                      false, tt)
+                        : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false,
+                                                      v == 1, tt)
                         : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs)
                                      : false;
         if (ok) c->g = g;
@@ -913,7 +1026,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
       q = comma + 1;
     }
     c->gen++;
-    c->plan = plan_json(c, "\"pinned\"");
+    c->plan = "\"pinned\"";
     return PFDD_OK;
   }
   if (c->tune) {
@@ -926,12 +1039,12 @@ static pfdd_status autotune(pfdd_ctx *c) {
         Geometry g = c->g;
         if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
             set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide,
-                           it->second.xWarp) &&
+                           it->second.xWarp, uses_tile_table(c->prec) ? c->ntiles : 0) &&
             (c->n[1] == 1 ||
              set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs))) {
           c->g = g;
           c->gen++;
-          c->plan = plan_json(c, "{\"cached\": true, \"timings\": " + it->second.timings + "}");
+          c->plan = "{\"cached\": true, \"timings\": " + it->second.timings + "}";
           return PFDD_OK;
         }
       }
@@ -991,7 +1104,9 @@ static pfdd_status autotune(pfdd_ctx *c) {
       const int lgT = cand / 3, form = cand % 3;
       const bool wide = form == 1, warp = form == 2;
       Geometry g = c->g;
-      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide, warp)) continue;
+      if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide, warp,
+                          uses_tile_table(c->prec) ? c->ntiles : 0))
+        continue;
       c->g = g;
       const double us = time_us([&] { return launch_x_fused<T>(c); });
       if (us > 0 && us < bt) { bt = us; best = g; }
@@ -1032,7 +1147,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }
-  c->plan = plan_json(c, tuning);
+  c->plan = tuning;
   return PFDD_OK;
 }
 
@@ -1150,7 +1265,7 @@ extern "C" pfdd_status pfdd_step(pfdd_ctx *c, int nsteps, const double *tau, dou
 
 extern "C" pfdd_status pfdd_get_plan(pfdd_ctx *c, char *buf, size_t len) {
   if (!c || !buf || len == 0) return fail(c, PFDD_EINVAL, "pfdd_get_plan: bad argument");
-  const std::string p = c->tuned ? c->plan : plan_json(c, "null");
+  const std::string p = plan_json(c, c->tuned ? c->plan : std::string("null"));
   if (p.size() + 1 > len) return fail(c, PFDD_EINVAL, "pfdd_get_plan: buffer of %zu bytes, need %zu", len, p.size() + 1);
   std::memcpy(buf, p.c_str(), p.size() + 1);
   return PFDD_OK;

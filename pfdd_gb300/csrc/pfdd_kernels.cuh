@@ -385,17 +385,48 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
   }
 }
 
-// Device order of B(k).  The fused x-pass tile c (T consecutive inner indices
-// j*N3+k, every x) holds B for its T*N1 points contiguously per pair:
+// Device order of B(k), by fused x-pass tile (every x of its inner indices
+// c = j*N3 + k), each tile one contiguous block.
+// Consecutive tiles (tiles == null): tile c holds T consecutive inner indices,
 //   index = (c*P + p) * (T*N1) + t*N1 + x,  inner index = c*T + t.
+// Tile table (the FP32 stored-table form): tile i holds the lines tiles[i] =
+// (ca, cb) from offset toff[i].  B(k) built from the closed form satisfies
+// B(-k) = B(k) bit for bit (every product in it is even in f), and the point
+// mirrored through the origin, ((N1-x)%N1, (N2-j)%N2, (N3-k)%N3), has
+// frequency -f unless one of its indices is a Nyquist index N/2 (its own
+// mirror with a nonzero frequency; for N = 1 index 0, which frec maps to -1).
+// So a line ca with j and k below Nyquist and its mirror line
+// cb = m(ca) form one "mirrored" tile that stores only ca's row per pair, W =
+// b_wm(N1) values: x < N1 for ca, and at x = N1 the value of cb at its Nyquist
+// x = N1/2 (the one point of cb that is not a mirror of ca); cb's other points
+// read ca's row at (N1 - x) % N1.  Other lines are "single" tiles (cb = -1)
+// of one row of W = N1 rounded up to 4 per pair.  A B(k) given by the caller
+// that lacks the symmetry gets single tiles only.  line_tile[c] = tile*2 + role
+// (0: ca, 1: cb).
 struct BLayout {
   long long N, inner;
   int L, lgT, P;
+  const int2 *tiles;          // null: consecutive tiles
+  const long long *toff;      // [ntiles + 1] offsets (values)
+  const int *line_tile;       // [inner]
 };
+__host__ __device__ __forceinline__ int b_mirror(int i, int n) { return (n - i) & (n - 1); }
+// row width of a mirrored tile (N1 values + the Nyquist column, a multiple of
+// 4 so every block is a whole number of 16-byte units)
+__host__ __device__ __forceinline__ int b_wm(int L) { return (L + 4) / 4 * 4; }
+// -1: not stored (the mirror's value, see BLayout)
 __host__ __device__ __forceinline__ long long b_index(const BLayout &bl, int p, long long pt) {
   const long long x = pt / bl.inner, c = pt - x * bl.inner;
-  const long long tile = c >> bl.lgT, t = c & ((1LL << bl.lgT) - 1);
-  return (tile * bl.P + p) * ((long long)bl.L << bl.lgT) + t * bl.L + x;
+  if (!bl.tiles) {
+    const long long tile = c >> bl.lgT, t = c & ((1LL << bl.lgT) - 1);
+    return (tile * bl.P + p) * ((long long)bl.L << bl.lgT) + t * bl.L + x;
+  }
+  const int lt = bl.line_tile[c], tile = lt >> 1, role = lt & 1;
+  const long long base = bl.toff[tile];
+  if (bl.tiles[tile].y < 0) return base + (long long)p * ((bl.toff[tile + 1] - base) / bl.P) + x;
+  const long long W = b_wm(bl.L);
+  if (role == 0) return base + p * W + x;
+  return x == bl.L / 2 ? base + p * W + bl.L : -1;
 }
 
 // Constants of the closed-form B(k) for the x-pass that evaluates the
@@ -414,6 +445,10 @@ struct BFlyParams {
 struct XParams {
   void *S;
   const void *B;
+  const int2 *xt;            // tile table (null: tiles of T consecutive inner indices), see BLayout
+  const long long *xtoff;
+  const int *xline;          // line -> tile * 2 + role
+  const int *xord;           // T = 1: the CTA's line (lines tile by tile)
   const uint8_t *active;
   const void *tw;          // x-axis forward twiddles (length L = N1)
   long long inner, tiles;  // inner = N2*N3, tiles = inner / T per field row
@@ -432,11 +467,11 @@ __device__ __forceinline__ float frec_f(int i, int n, float d) {
 }
 
 // k-space contraction of one point, S_a <- sum_b B_ab S_b (F:4609-4629, b
-// ascending), with the point's B(k) in the shared-memory tile Bs (P pairs a <=
-// b, npt points each).  at(a) is the point's value of field a (read, then
+// ascending), with the point's B(k) in the shared-memory tile Bs: pair p's
+// value at Bs[p * W + bx].  at(a) is the point's value of field a (read, then
 // overwritten).  IN_REGS keeps the NS inputs in registers.
 template <typename T, int NS, bool IN_REGS, typename At>
-__device__ __forceinline__ void contract_table(const T *Bs, int npt, int q, At at) {
+__device__ __forceinline__ void contract_table(const T *Bs, int W, int bx, At at) {
   using V = typename cpx<T>::t;
   V out[NS];
   V in[IN_REGS ? NS : 1];
@@ -451,7 +486,7 @@ __device__ __forceinline__ void contract_table(const T *Bs, int npt, int q, At a
     const V ina = IN_REGS ? in[a] : at(a);
 #pragma unroll
     for (int b = a; b < NS; ++b, ++pidx) {
-      const T v = Bs[pidx * npt + q];
+      const T v = Bs[pidx * W + bx];
       const V inb = IN_REGS ? in[b] : at(b);
       out[a].x += inb.x * v;
       out[a].y += inb.y * v;
@@ -539,11 +574,12 @@ __device__ __forceinline__ void contract_bfly(const BFlyParams &bf, At at, int x
 }
 
 // Shared-memory bytes of the fused x-pass for a tile of T = 2^lgT.
+// table: the tile-table layout (T = 2, B rows of at most L + 4 values).
 __host__ __device__ __forceinline__ size_t x_fused_smem(int ns, int L, int lgT, int pitch, size_t vsize,
-                                                        size_t bsize) {
+                                                        size_t bsize, bool table = false) {
   const size_t head = ((size_t)L + (size_t)ns * ((size_t)1 << lgT) * pitch) * vsize;
   const size_t P = (size_t)ns * (ns + 1) / 2;
-  return ((head + 15) & ~(size_t)15) + P * ((size_t)L << lgT) * bsize;
+  return ((head + 15) & ~(size_t)15) + P * (table ? (size_t)L + 4 : ((size_t)L << lgT)) * bsize;
 }
 
 // Fused x-pass on a tile of T consecutive inner indices, all N1 x-values and
@@ -577,7 +613,6 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   const long long c0 = tile << lgT;
   const int npt = L << lgT;
   V *S = reinterpret_cast<V *>(p.S);
-  const T *Bt = reinterpret_cast<const T *>(p.B) + tile * P * (long long)npt;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nel = (NS * L) << lgT;
   auto sidx = [&](int a, int t, int x) { return (a * TT + t) * LP + x; };
@@ -585,53 +620,86 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   const int E = L >= NV ? NV : L, team = L / E, teams = nthr / team;
   const int lines = NS << lgT;
   const int my_team = tid % teams, th = tid / teams;  // consecutive lanes on consecutive lines
+  // tile table (see BLayout): T = 2, a CTA per tile (its lines ca and cb in
+  // slots 0 and 1, slot 1 empty for a single tile); T = 1, a CTA per line
+  // (xord lists the lines tile by tile, so the two CTAs of a mirrored tile
+  // run back to back and the second reads the shared B block from L2)
+  int2 tp = make_int2(0, 0);
+  long long tix = tile;
+  int role0 = 0;
+  if (p.xt) {
+    if (lgT == 0) {
+      const int c = p.xord[tile], lt = p.xline[c];
+      tix = lt >> 1;
+      role0 = lt & 1;
+      tp = make_int2(c, -1);
+    } else {
+      tp = p.xt[tile];
+    }
+  }
+  const int tl = p.xt && tp.y < 0 ? 1 : TT;
+  auto cidx = [&](int t) { return p.xt ? (t ? tp.y : tp.x) : (int)(c0 + t); };
+  const long long boff = p.xt ? p.xtoff[tix] : tile * P * (long long)npt;
+  const int bvals = p.xt ? (int)(p.xtoff[tix + 1] - boff) : P * npt;
+  const bool mirrored = p.xt && p.xt[tix].y >= 0;
+  const int W = p.xt ? (mirrored ? b_wm(L) : bvals / P) : npt;
+  const T *Bt = reinterpret_cast<const T *>(p.B) + boff;
   // S is x-fastest: line (a, t) of the tile is L contiguous values; consecutive
   // lanes copy consecutive x (whole 128-byte lines per warp)
   // element x of tile line ln sits at Sr[goff(ln) + x]: 32-bit offsets from the
-  // tile's base (a replica's ns fields hold fewer than 2^31 values)
-  V *Sr = S + ((long long)r * NS * p.inner + c0) * L;
+  // replica's base (a replica's ns fields hold fewer than 2^31 values)
+  V *Sr = S + (long long)r * NS * p.inner * L;
   const int fstride = (int)p.inner * L;
-  auto goff = [&](int ln) { return (ln >> lgT) * fstride + (ln & (TT - 1)) * L; };
+  auto goff = [&](int ln) { return (ln >> lgT) * fstride + cidx(ln & (TT - 1)) * L; };
+  auto live = [&](int ln) { return (ln & (TT - 1)) < tl; };
   for (int e = tid; e < nel; e += nthr) {
     const int x = e & (L - 1), ln = e >> lgL;
-    cp_async_elem(&sm[ln * LP + x], Sr + goff(ln) + x);
+    if (live(ln)) cp_async_elem(&sm[ln * LP + x], Sr + goff(ln) + x);
   }
   cp_async_commit();
-  // B tile: one contiguous block of P * npt values, TMA bulk copies issued by
+  // B tile: one contiguous block of bvals values, TMA bulk copies issued by
   // one thread so it streams in during the forward FFT
   __shared__ __align__(8) uint64_t bbar;
-  const int bbytes = BFLY ? 0 : P * npt * (int)sizeof(T);
-  const bool bulk = !BFLY && (bbytes & 15) == 0;
+  const int bbytes = BFLY ? 0 : bvals * (int)sizeof(T);
+  const bool bulk = !BFLY && (bbytes & 15) == 0 && ((boff * (long long)sizeof(T)) & 15) == 0;
   if (bulk && tid == 0) {
     mbar_init(&bbar, 1);
     bulk_load(Bs, Bt, (unsigned)bbytes, &bbar);
   }
   if (!BFLY && !bulk)
-    for (int i = tid; i < P * npt; i += nthr) Bs[i] = Bt[i];
+    for (int i = tid; i < bvals; i += nthr) Bs[i] = Bt[i];
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   cp_async_wait<0>();
   __syncthreads();
   for (int l0 = 0; l0 < lines; l0 += teams) {
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-    line_fft<-1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+    line_fft<-1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines && live(ln));
   }
   if (bulk) mbar_wait(&bbar, 0, p.err);
   __syncthreads();
-  for (int q = tid; q < npt; q += nthr) {
+  for (int q = tid; q < (tl << lgL); q += nthr) {
     const int t = q >> lgL, x = q & (L - 1);
     auto at = [&](int a) -> V & { return sm[sidx(a, t, x)]; };
-    if constexpr (BFLY) contract_bfly<NS>(p.bf, at, x, L, c0 + t);
-    else contract_table<T, NS, IN_REGS>(Bs, npt, q, at);
+    if constexpr (BFLY) {
+      contract_bfly<NS>(p.bf, at, x, L, c0 + t);
+    } else {
+      // the point's column in the B block: consecutive tiles q; tile table
+      // x, or for a mirrored tile's second line the mirror x (its Nyquist x
+      // has a column of its own)
+      const int role = lgT == 0 ? role0 : t;
+      const int bx = !p.xt ? q : (role == 0 ? x : (x == L / 2 ? L : b_mirror(x, L)));
+      contract_table<T, NS, IN_REGS>(Bs, W, bx, at);
+    }
   }
   __syncthreads();
   for (int l0 = 0; l0 < lines; l0 += teams) {
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
-    line_fft<+1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines);
+    line_fft<+1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines && live(ln));
   }
   __syncthreads();
   for (int e = tid; e < nel; e += nthr) {
     const int x = e & (L - 1), ln = e >> lgL;
-    Sr[goff(ln) + x] = sm[ln * LP + x];
+    if (live(ln)) Sr[goff(ln) + x] = sm[ln * LP + x];
   }
 }
 
@@ -713,7 +781,7 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
     const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
     auto at = [&](int a) -> V & { return sm[(a * TT + t) * LP + sx]; };
     if constexpr (BFLY) contract_bfly<NS>(p.bf, at, x, L, c0 + t);
-    else contract_table<float, NS, true>(Bs, npt, q, at);
+    else contract_table<float, NS, true>(Bs, npt, q, at);  // consecutive tiles only
   }
   __syncthreads();
   for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {

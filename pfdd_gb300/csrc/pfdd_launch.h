@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "pfdd_kernels.cuh"
 
@@ -67,9 +68,10 @@ struct Geometry {
   int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1};
   long long tiles[2] = {1, 1};
   size_t smem[2] = {0, 0};
-  // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel)
+  // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel); xTable: the
+  // B(k) tile-table layout (see BLayout), xTiles then the table's tile count
   int xLgT = 0, xPitch = 1, xThreads = 256;
-  bool xWide = false, xWarp = false;
+  bool xWide = false, xWarp = false, xTable = false;
   long long xTiles = 1;
   size_t xSmem = 0;
 };
@@ -120,10 +122,13 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
 // phases (16 lanes of 8 bytes, 8 of 16 bytes), i.e. every phase of an FFT
 // stage touches as many different lines as it has lanes (no bank conflicts),
 // at the price of idle threads when the tile has fewer lines.
+// table_tiles > 0: the tile-table layout with that many tiles (the block-team
+// kernel only; T = 2: a CTA per tile, T = 1: a CTA per line).
 inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT,
-                           bool wide = false, bool warp = false) {
+                           bool wide = false, bool warp = false, long long table_tiles = 0) {
   const long long innerx = (long long)n2 * n3;
-  if ((1LL << lgT) > innerx) return false;
+  if ((1LL << lgT) > innerx && table_tiles == 0) return false;
+  if (table_tiles > 0 && (lgT > 1 || warp)) return false;
   if (warp) {  // FP32 spectra, N1 = 32..256; a thread a point, at most 384
     const int lgL = ilog2(n1);
     if (wide || vsize != 8 || n1 < 32 || n1 > 256) return false;
@@ -139,11 +144,12 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
     g.xThreads = thr;
     g.xWide = false;
     g.xWarp = true;
+    g.xTable = false;
     return true;
   }
   g.xWarp = false;
   const int pitch = line_pitch(n1);
-  const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize);
+  const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize, table_tiles > 0);
   if (smem > kMaxDynSmem) return false;
   const int team = x_line_team(n1, vsize), lines = ns << lgT, npt = n1 << lgT;
   const int unit = std::max(32, team);
@@ -156,7 +162,8 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
   thr = (thr + unit - 1) / unit * unit;
   g.xPitch = pitch;
   g.xLgT = lgT;
-  g.xTiles = innerx >> lgT;
+  g.xTiles = table_tiles > 0 ? (lgT == 1 ? table_tiles : innerx) : innerx >> lgT;
+  g.xTable = table_tiles > 0;
   g.xSmem = smem;
   g.xThreads = std::min(thr, cap / unit * unit);
   g.xWide = wide;
@@ -167,7 +174,8 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
 // value, 0 when the x-pass evaluates B(k) itself.  The strided and x-pass tile
 // widths chosen here are the defaults; a context's first step may retune them
 // (they do not change any result).
-inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, bool xfast = false) {
+inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, bool xfast = false,
+                              long long table_tiles = 0) {
   Geometry g;
   g.xfast = xfast;
   const int L3 = n3, team3 = z_line_team(L3, vsize);
@@ -189,9 +197,48 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
     while (lgT > 0 && ((1LL << lgT) > (long long)n2 * n3 ||
                        x_fused_smem(ns, n1, lgT, line_pitch(n1), vsize, bsize) > 110 * 1024))
       --lgT;
-    g.valid = set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
+    g.valid = table_tiles > 0 ? set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 1, false, false, table_tiles)
+                              : set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
   }
   return g;
+}
+
+// B(k) tile table (see BLayout): symmetric: a mirrored tile for each line pair
+// (c, m(c)) whose indices j, k are below Nyquist (c != m(c)), single tiles for
+// the other lines; otherwise single tiles only.  Offsets in values.
+struct TileTable {
+  std::vector<int2> tiles;
+  std::vector<long long> toff;
+  std::vector<int> line_tile, order;  // order: the lines tile by tile
+};
+inline TileTable make_tile_table(int n1, int n2, int n3, int P, bool symmetric) {
+  TileTable t;
+  const int inner = n2 * n3;
+  t.line_tile.assign(inner, -1);
+  const long long ws = (n1 + 3) / 4 * 4, wm = b_wm(n1);
+  auto nyq = [](int i, int n) { return i == n / 2; };  // its own mirror, nonzero frequency
+  long long off = 0;
+  for (int c = 0; c < inner; ++c) {
+    if (t.line_tile[c] >= 0) continue;  // the second line of a mirrored tile
+    const int j = c / n3, k = c % n3, m = b_mirror(j, n2) * n3 + b_mirror(k, n3);
+    const int id = (int)t.tiles.size();
+    t.toff.push_back(off);
+    if (symmetric && !nyq(j, n2) && !nyq(k, n3) && m != c) {
+      t.tiles.push_back(make_int2(c, m));
+      t.line_tile[c] = 2 * id;
+      t.line_tile[m] = 2 * id + 1;
+      t.order.push_back(c);
+      t.order.push_back(m);
+      off += P * wm;
+    } else {
+      t.tiles.push_back(make_int2(c, -1));
+      t.line_tile[c] = 2 * id;
+      t.order.push_back(c);
+      off += P * ws;
+    }
+  }
+  t.toff.push_back(off);
+  return t;
 }
 
 // Per-kernel record of the dynamic shared memory opted into on each device.

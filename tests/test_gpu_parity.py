@@ -71,6 +71,64 @@ def test_device_B_matches_reference_formula(native_lib):
             assert np.max(np.abs(Bg - Bo)) <= 1e-13 * max(1.0, np.max(np.abs(Bo)))
 
 
+@pytest.mark.parametrize("n", [(8, 16, 4), (32, 32, 32), (2, 8, 1), (1, 16, 8), (16, 1, 2), (128, 8, 16)])
+def test_fp32_tile_table_B_matches_reference_formula(native_lib, n):
+    """The FP32 stored-table form keeps one of each pair of mirrored points
+    (B(-k) = B(k)); every point read back equals the formula rounded to FP32."""
+    eps = oracle.fcc_eps(12)
+    Bo = oracle.bmatrix(n, eps, 3.5, 1.5, 1.0)
+    s = native.Solver(n, 12, "fp32")
+    s.build_B(3.5, 1.5, 1.0, eps)
+    Bg = s.get_B()
+    xp = s.plan()["x_pass"]
+    s.close()
+    assert np.max(np.abs(Bg - Bo)) <= 1.2e-7 * max(1.0, np.max(np.abs(Bo)))
+    assert xp["b_mirrored"] == 1 and xp["b_tiles"] <= n[1] * n[2]
+
+
+def test_fp32_tile_table_with_asymmetric_B(native_lib):
+    """A caller's B(k) without the mirror symmetry switches the FP32 table
+    form to single tiles: the step still matches the FP64 form given the
+    same B(k), and a symmetric B(k) through the host path gives the device
+    build's bits."""
+    spec = workloads.SolveSpec(n=(16, 8, 16), ns=12, steps=8, sigma_max=0.05,
+                               loops=workloads.random_loops((16, 8, 16), 3, 2.0, 5.0, 12, seed=5), noise_seed=5)
+    eps = oracle.fcc_eps(12)
+    Bo = oracle.bmatrix(spec.n, eps, 3.5, 1.5, 1.0)
+    x0, b0 = workloads.initial_state(spec)
+    tau = native.spec_tau(spec)
+
+    def run(prec, B=None):
+        s = native.Solver(spec.n, 12, prec)
+        if B is None:
+            s.build_B(3.5, 1.5, 1.0, eps)
+        else:
+            s.set_B(B)
+        s.set_params(0.01, 0.1, 1.0)
+        s.set_state(x0, b0)
+        g, _ = s.step(tau)
+        xp = s.plan()["x_pass"]
+        out = (g[:, 0], s.get_state()[0], (xp["b_tiles"], xp["b_mirrored"]), s.get_B())
+        s.close()
+        return out
+
+    g_dev, x_dev, lay_dev, B_dev = run("fp32")
+    assert lay_dev[1] == 1 and lay_dev[0] < 8 * 16
+    # the device-built values through the host path: the same table, the same bits
+    g_host, x_host, lay_host, _ = run("fp32", B_dev)
+    np.testing.assert_array_equal(g_host, g_dev)
+    np.testing.assert_array_equal(x_host, x_dev)
+    assert lay_host == lay_dev
+    Ba = Bo.copy()
+    Ba[0, 0, 3, 2, 5] *= 1.01  # one point no longer equals its mirror
+    g_a, x_a, lay_a, B_back = run("fp32", Ba)
+    g_64, x_64, _, _ = run("fp64", Ba)
+    assert lay_a == (8 * 16, 0)  # one tile per line
+    assert np.max(np.abs(B_back - Ba)) <= 1.2e-7 * np.max(np.abs(Ba))
+    assert np.max(np.abs(x_a - x_64)) <= 1e-6
+    assert rel(g_a, g_64) <= 1e-5
+
+
 def test_set_B_host_path_equals_device_build(native_lib):
     spec = workloads.SolveSpec(n=(16, 8, 16), ns=12, steps=6, sigma_max=0.05,
                                loops=workloads.random_loops((16, 8, 16), 3, 2.0, 5.0, 12, seed=3), noise_seed=3)

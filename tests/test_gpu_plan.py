@@ -102,7 +102,7 @@ def pinned(spec, precision, plan, nrep=1, prepare=None):
     return out
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp32_bfly"])
+@pytest.mark.parametrize("precision", ["fp32_bfly"])
 def test_warp_team_xpass_batched_pinned_and_idle(native_lib, precision):
     """The warp-team x-pass on a batch: an idle replica whose tiles are
     skipped, pinned points, N1 = 128."""
@@ -121,13 +121,14 @@ def test_warp_team_xpass_batched_pinned_and_idle(native_lib, precision):
     assert res[0][2]["x_pass"]["warp_teams"] == 1
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp32_bfly"])
+@pytest.mark.parametrize("precision", ["fp32_bfly"])
 @pytest.mark.parametrize("n1,plan", [(32, "x=1,w=1"), (64, "x=2,w=1"), (128, "x=1,w=1"), (128, "x=4,w=1"),
                                      (256, "x=1,w=1")])
 def test_warp_team_xpass_gives_same_bits(native_lib, precision, n1, plan):
     """The warp-team x-pass (lines straight between global memory and
     registers, warp-local FFT stages, swizzled shared-memory lines) computes
-    the block-team x-pass's bits, with a stored B(k) and with B(k) in registers."""
+    the block-team x-pass's bits (B(k) in registers; the stored-table form
+    runs the block-team kernel on its tile table)."""
     n = (n1, 8, 16)
     spec = workloads.SolveSpec(n=n, ns=12, steps=6, sigma_max=0.05, noise_seed=33,
                                loops=workloads.random_loops(n, 3, 1.5, 3.0, 12, seed=33))
@@ -137,3 +138,18 @@ def test_warp_team_xpass_gives_same_bits(native_lib, precision, n1, plan):
     assert p1["x_pass"]["tile_columns"] == int(plan.split(",")[0][2:])
     np.testing.assert_array_equal(g1, g0)
     np.testing.assert_array_equal(x1, x0)
+
+
+@pytest.mark.parametrize("n", [(128, 8, 16), (32, 16, 8), (16, 2, 4)])
+def test_table_form_line_and_pair_ctas_same_bits(native_lib, n):
+    """The FP32 stored-table form's two x-pass shapes on the mirrored B(k)
+    tile table -- a CTA per line and a CTA per mirrored pair -- give the same
+    bits."""
+    spec = workloads.SolveSpec(n=n, ns=12, steps=6, sigma_max=0.05, noise_seed=34,
+                               loops=workloads.random_loops(n, 2, 1.0, 2.0, 12, seed=34))
+    g1, x1, p1 = pinned(spec, "fp32", "x=1")
+    g2, x2, p2 = pinned(spec, "fp32", "x=2")
+    assert (p1["x_pass"]["tile_columns"], p2["x_pass"]["tile_columns"]) == (1, 2)
+    assert p1["x_pass"]["b_mirrored"] == p2["x_pass"]["b_mirrored"] == 1
+    np.testing.assert_array_equal(g1, g2)
+    np.testing.assert_array_equal(x1, x2)
