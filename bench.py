@@ -151,11 +151,29 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # our arm
 
-def algorithmic_bytes(kernel: str, prec: str, n_pts: int, rf: int, ns: int) -> float:
-    """Compulsory DRAM bytes of one launch (read + write once what the kernel must touch)."""
-    v = 16 if prec == "fp64" else 8          # complex spectral element
-    b = 8 if prec == "fp64" else 4           # B(k) element
+def b_table_bytes(prec: str, n, ns: int, plan: dict | None = None) -> float:
+    """Bytes of the stored B(k): FP64 P*N values; the FP32 table form's tile
+    table (one row of N1+4 per pair for a mirrored line pair, N1 rounded up to
+    4 per single line: pairs = inner - tiles, singles = 2 tiles - inner);
+    none when B(k) is evaluated in the x-pass."""
     P = ns * (ns + 1) // 2
+    n1, n2, n3 = n
+    if prec == "fp32_bfly":
+        return 0.0
+    if prec == "fp64":
+        return P * n1 * n2 * n3 * 8.0
+    xp = (plan or {}).get("x_pass", {})
+    tiles, inner = xp.get("b_tiles", 0), n2 * n3
+    if not tiles:
+        return P * n1 * n2 * n3 * 4.0
+    pairs, singles = inner - tiles, 2 * tiles - inner
+    return P * ((n1 + 4) // 4 * 4 * pairs + (n1 + 3) // 4 * 4 * singles) * 4.0
+
+
+def algorithmic_bytes(kernel: str, prec: str, n_pts: int, rf: int, ns: int, b_bytes: float = 0.0) -> float:
+    """Compulsory DRAM bytes of one launch (read + write once what the kernel
+    must touch); b_bytes: the stored B(k) the x-pass reads."""
+    v = 16 if prec == "fp64" else 8          # complex spectral element
     if kernel in ("z_step", "plane"):
         return rf * n_pts * (2 * v + 32)     # S in/out + FP64 xi in/out
     if kernel in ("z_prologue", "plane_prologue"):
@@ -163,7 +181,7 @@ def algorithmic_bytes(kernel: str, prec: str, n_pts: int, rf: int, ns: int) -> f
     if kernel.startswith("fft_"):
         return rf * n_pts * 2 * v
     if kernel in ("contract", "x_fused"):
-        return rf * n_pts * 2 * v + (0 if prec == "fp32_bfly" else P * n_pts * b)
+        return rf * n_pts * 2 * v + b_bytes
     return 0.0
 
 
@@ -541,14 +559,14 @@ def run_ours(a):
             kern[nm] = {"launches": cnt, "avg_us": 1e3 * tot / cnt}
         cnt, tot = ks[top]
         avg_s = tot / cnt / 1e3
-        ab = algorithmic_bytes(top, head, spec.npts, spec.ns, spec.ns)
+        ab = algorithmic_bytes(top, head, spec.npts, spec.ns, spec.ns, b_table_bytes(head, spec.n, spec.ns, rh["plan"]))
         ach = ab / avg_s / 1e9
         tr = profiled_traffic(top, head, a.n, spec.ns)
         roof = {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": tr, "algorithmic_bytes": ab,
                 "peak_src": peaks["src"] + " (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback"}
     # compulsory bytes of a step: xi in and out (and the B(k) table when stored)
-    step_bytes = spec.npts * (spec.ns * 32 + (0 if head == "fp32_bfly" else spec.ns * (spec.ns + 1) // 2 * 4))
+    step_bytes = spec.npts * spec.ns * 32 + b_table_bytes(head, spec.n, spec.ns, rh["plan"])
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not a.no_cpu_baseline and r64["B"] is not None:
         cpu = cpu_baseline_port(spec, r64["B"])
@@ -583,7 +601,9 @@ def run_ours(a):
                    "form": head, "grid": [a.n] * 3, "ns": spec.ns, "solves_per_gpu": 1, "global_batch": dist.world,
                    "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2 (xi 403 MB + S 201 MB per step"
-                         + ("" if head == "fp32_bfly" else " + B 327 MB") + ", L2 126 MB)"},
+                         + ("" if head == "fp32_bfly" else
+                            f" + B(k) table {b_table_bytes(head, spec.n, spec.ns, rh['plan']) / 1e6:.0f} MB")
+                         + ", L2 126 MB)"},
         "updates_per_s": round(vh * spec.npts * spec.ns, 1),
         "hbm_roofline_step": {"algorithmic_bytes_per_step": step_bytes,
                               "achieved_gbs": round(step_bytes * vh / dist.world / 1e9, 1),
