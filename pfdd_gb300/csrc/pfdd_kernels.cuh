@@ -601,7 +601,10 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   using V = typename cpx<T>::t;
   constexpr int P = NS * (NS + 1) / 2;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int L = p.L, lgL = p.lgL, lgT = p.lgT, TT = 1 << lgT, LP = p.pitch;
+  // line length and pitch fixed at compile time when LG is (the host's pitch
+  // is line_pitch(N1) = N1 + 1), so the shared-memory addressing folds
+  const int L = LG >= 0 ? 1 << LG : p.L, lgL = LG >= 0 ? LG : p.lgL, lgT = p.lgT, TT = 1 << lgT;
+  const int LP = LG >= 0 ? (1 << LG) + 1 : p.pitch;
   V *tws = reinterpret_cast<V *>(smraw);
   V *sm = tws + L;
   const size_t head = (((size_t)L + (size_t)NS * TT * LP) * sizeof(V) + 15) & ~(size_t)15;
