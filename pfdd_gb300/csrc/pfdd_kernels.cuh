@@ -721,10 +721,10 @@ __host__ __device__ __forceinline__ int xw_swz(int l, int lgL) {
 
 // Shared-memory bytes of the warp-team x-pass: twiddles | tile lines |
 // B tile (bsize 0: B evaluated in registers).
-__host__ __device__ __forceinline__ size_t xw_smem(int ns, int lgL, int lgT, size_t bsize) {
+__host__ __device__ __forceinline__ size_t xw_smem(int ns, int lgL, int lgT, size_t bsize, bool table = false) {
   const size_t head = (((size_t)1 << lgL) + (size_t)ns * ((size_t)1 << lgT) * xw_pitch(lgL)) * 8;
   const size_t P = (size_t)ns * (ns + 1) / 2;
-  return ((head + 15) & ~(size_t)15) + P * ((size_t)1 << (lgL + lgT)) * bsize;
+  return ((head + 15) & ~(size_t)15) + P * (table ? ((size_t)1 << lgL) + 4 : (size_t)1 << (lgL + lgT)) * bsize;
 }
 
 // Fused x-pass with warp-resident line teams (FP32 spectra, N1 = 32..256):
@@ -755,19 +755,42 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   const long long c0 = tile << lgT;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
   const int th = lane & (LV - 1), wl = lane / LV;  // team thread, line of the warp
-  V *Sr = reinterpret_cast<V *>(p.S) + ((long long)r * NS * p.inner + c0) * L;
+  // tile table (stored-table form, see BLayout and x_fused_kernel): T = 2, a
+  // CTA per tile; T = 1, a CTA per line
+  int2 tp = make_int2(0, 0);
+  long long tix = tile;
+  int role0 = 0;
+  if (!BFLY && p.xt) {
+    if (lgT == 0) {
+      const int c = p.xord[tile], lt = p.xline[c];
+      tix = lt >> 1;
+      role0 = lt & 1;
+      tp = make_int2(c, -1);
+    } else {
+      tp = p.xt[tile];
+    }
+  }
+  const bool tabled = !BFLY && p.xt;
+  const int tl = tabled && tp.y < 0 ? 1 : TT;
+  auto cidx = [&](int t) { return tabled ? (t ? tp.y : tp.x) : (int)(c0 + t); };
+  auto live = [&](int ln) { return (ln & (TT - 1)) < tl; };
+  const long long boff = tabled ? p.xtoff[tix] : tile * P * (long long)npt;
+  const int bvals = BFLY ? 0 : (tabled ? (int)(p.xtoff[tix + 1] - boff) : P * npt);
+  const bool mirrored = tabled && p.xt[tix].y >= 0;
+  const int W = tabled ? (mirrored ? b_wm(L) : bvals / P) : npt;
+  V *Sr = reinterpret_cast<V *>(p.S) + (long long)r * NS * p.inner * L;
   const int fstride = (int)p.inner * L;
-  auto goff = [&](int ln) { return (ln >> lgT) * fstride + (ln & (TT - 1)) * L; };
+  auto goff = [&](int ln) { return (ln >> lgT) * fstride + cidx(ln & (TT - 1)) * L; };
   __shared__ __align__(8) uint64_t bbar;
-  if (!BFLY && tid == 0) {  // B tile: P * npt contiguous values (a multiple of 16 bytes)
+  if (!BFLY && tid == 0) {  // B tile: bvals contiguous values (a multiple of 16 bytes)
     mbar_init(&bbar, 1);
-    bulk_load(Bs, reinterpret_cast<const float *>(p.B) + tile * P * (long long)npt, (unsigned)(P * npt * 4), &bbar);
+    bulk_load(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
   }
   load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   __syncthreads();  // twiddles (the second stage on) and the barrier's initialisation
   for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
     const int ln = ln0 + wl;
-    const bool act = ln < lines;
+    const bool act = ln < lines && live(ln);
     V *line = sm + ln * LP;
     V v[NV];
     if (act) {
@@ -780,16 +803,21 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   }
   if (!BFLY) mbar_wait(&bbar, 0, p.err);
   __syncthreads();
-  for (int q = tid; q < npt; q += nthr) {
+  for (int q = tid; q < (tl << LG); q += nthr) {
     const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
     auto at = [&](int a) -> V & { return sm[(a * TT + t) * LP + sx]; };
-    if constexpr (BFLY) contract_bfly<NS>(p.bf, at, x, L, c0 + t);
-    else contract_table<float, NS, true>(Bs, npt, q, at);  // consecutive tiles only
+    if constexpr (BFLY) {
+      contract_bfly<NS>(p.bf, at, x, L, c0 + t);
+    } else {
+      const int role = lgT == 0 ? role0 : t;
+      const int bx = !tabled ? q : (role == 0 ? x : (x == L / 2 ? L : b_mirror(x, L)));
+      contract_table<float, NS, true>(Bs, W, bx, at);
+    }
   }
   __syncthreads();
   for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
     const int ln = ln0 + wl;
-    const bool act = ln < lines;
+    const bool act = ln < lines && live(ln);
     V *line = sm + ln * LP;
     V *g = Sr + (act ? goff(ln) : 0);
     V v[NV];

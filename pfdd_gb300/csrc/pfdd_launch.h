@@ -122,29 +122,29 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
 // phases (16 lanes of 8 bytes, 8 of 16 bytes), i.e. every phase of an FFT
 // stage touches as many different lines as it has lanes (no bank conflicts),
 // at the price of idle threads when the tile has fewer lines.
-// table_tiles > 0: the tile-table layout with that many tiles (the block-team
-// kernel only; T = 2: a CTA per tile, T = 1: a CTA per line).
+// table_tiles > 0: the tile-table layout with that many tiles (T = 2: a CTA
+// per tile, T = 1: a CTA per line).
 inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT,
                            bool wide = false, bool warp = false, long long table_tiles = 0) {
   const long long innerx = (long long)n2 * n3;
   if ((1LL << lgT) > innerx && table_tiles == 0) return false;
-  if (table_tiles > 0 && (lgT > 1 || warp)) return false;
+  if (table_tiles > 0 && lgT > 1) return false;
   if (warp) {  // FP32 spectra, N1 = 32..256; a thread a point, at most 384
     const int lgL = ilog2(n1);
     if (wide || vsize != 8 || n1 < 32 || n1 > 256) return false;
-    const size_t smem = xw_smem(ns, lgL, lgT, bsize);
+    const size_t smem = xw_smem(ns, lgL, lgT, bsize, table_tiles > 0);
     if (smem > kMaxDynSmem) return false;
     const int lpw = 32 / xw_lv(lgL), lines = ns << lgT;
     int thr = std::max(n1 << lgT, (lines + lpw - 1) / lpw * 32);
     thr = std::min(384, (thr + 31) / 32 * 32);
     g.xPitch = xw_pitch(lgL);
     g.xLgT = lgT;
-    g.xTiles = innerx >> lgT;
+    g.xTiles = table_tiles > 0 ? (lgT == 1 ? table_tiles : innerx) : innerx >> lgT;
     g.xSmem = smem;
     g.xThreads = thr;
     g.xWide = false;
     g.xWarp = true;
-    g.xTable = false;
+    g.xTable = table_tiles > 0;
     return true;
   }
   g.xWarp = false;

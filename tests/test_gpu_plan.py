@@ -140,16 +140,19 @@ def test_warp_team_xpass_gives_same_bits(native_lib, precision, n1, plan):
     np.testing.assert_array_equal(x1, x0)
 
 
-@pytest.mark.parametrize("n", [(128, 8, 16), (32, 16, 8), (16, 2, 4)])
-def test_table_form_line_and_pair_ctas_same_bits(native_lib, n):
-    """The FP32 stored-table form's two x-pass shapes on the mirrored B(k)
-    tile table -- a CTA per line and a CTA per mirrored pair -- give the same
-    bits."""
+@pytest.mark.parametrize("n", [(128, 8, 16), (32, 16, 8), (16, 2, 4), (64, 4, 2)])
+@pytest.mark.parametrize("plan", ["x=1", "x=1,w=1", "x=2,w=1"])
+def test_table_form_line_and_pair_ctas_same_bits(native_lib, n, plan):
+    """The FP32 stored-table form's x-pass shapes on the mirrored B(k) tile
+    table -- a CTA per line or per mirrored pair, block or warp teams -- give
+    the same bits."""
     spec = workloads.SolveSpec(n=n, ns=12, steps=6, sigma_max=0.05, noise_seed=34,
                                loops=workloads.random_loops(n, 2, 1.0, 2.0, 12, seed=34))
-    g1, x1, p1 = pinned(spec, "fp32", "x=1")
+    g1, x1, p1 = pinned(spec, "fp32", plan)
     g2, x2, p2 = pinned(spec, "fp32", "x=2")
-    assert (p1["x_pass"]["tile_columns"], p2["x_pass"]["tile_columns"]) == (1, 2)
+    warp = "w=1" in plan and n[0] >= 32
+    assert p1["x_pass"]["tile_columns"] == int(plan.split(",")[0][2:]) and p2["x_pass"]["tile_columns"] == 2
+    assert p1["x_pass"]["warp_teams"] == int(warp) and p2["x_pass"]["warp_teams"] == 0
     assert p1["x_pass"]["b_mirrored"] == p2["x_pass"]["b_mirrored"] == 1
     np.testing.assert_array_equal(g1, g2)
     np.testing.assert_array_equal(x1, x2)
