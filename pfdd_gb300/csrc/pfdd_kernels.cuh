@@ -99,10 +99,10 @@ constexpr int kFixBits = 44;
 __device__ __forceinline__ long long to_fixed_bits(unsigned long long u, bool &big) {
   const int e = (int)((u >> 52) & 0x7ff);
   if (e >= 1023 + 7) { big = true; return 0; }
-  const int sh = 1075 - kFixBits - e;  // |d| = m * 2^(e-1075) = (m >> sh) units of 2^-44
-  if (e == 0 || sh >= 64) return 0;
+  const int sh = 1075 - kFixBits - e;  // |d| = m * 2^(e-1075) = (m >> sh) units of 2^-44; >= 2 here
+  if (sh >= 64) return 0;               // includes e == 0
   const unsigned long long m = (u & 0xfffffffffffffull) | (1ull << 52);
-  const long long v = sh > 0 ? (long long)((m + (1ull << (sh - 1))) >> sh) : (long long)(m << (-sh));
+  const long long v = (long long)((m + (1ull << (sh - 1))) >> sh);
   return (u >> 63) ? -v : v;
 }
 __device__ __forceinline__ long long to_fixed(double d, bool &big) {
@@ -609,8 +609,10 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   V *sm = tws + L;
   const size_t head = (((size_t)L + (size_t)NS * TT * LP) * sizeof(V) + 15) & ~(size_t)15;
   T *Bs = reinterpret_cast<T *>(smraw + head);
-  const long long r = blockIdx.x / p.tiles;
-  const long long tile = blockIdx.x - r * p.tiles;
+  // replicas of one tile on consecutive CTAs: a batch's CTAs that read the
+  // same B block run together, so it comes from HBM once and then from L2
+  const long long r = blockIdx.x % p.R;
+  const long long tile = blockIdx.x / p.R;
   if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
   if (p.active && !p.active[r]) return;
   const long long c0 = tile << lgT;
@@ -748,8 +750,10 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   V *sm = tws + L;
   const size_t head = (((size_t)L + (size_t)lines * LP) * sizeof(V) + 15) & ~(size_t)15;
   float *Bs = reinterpret_cast<float *>(smraw + head);
-  const long long r = blockIdx.x / p.tiles;
-  const long long tile = blockIdx.x - r * p.tiles;
+  // replicas of one tile on consecutive CTAs: a batch's CTAs that read the
+  // same B block run together, so it comes from HBM once and then from L2
+  const long long r = blockIdx.x % p.R;
+  const long long tile = blockIdx.x / p.R;
   if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
   if (p.active && !p.active[r]) return;
   const long long c0 = tile << lgT;
