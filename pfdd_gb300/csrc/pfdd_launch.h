@@ -197,7 +197,9 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
     while (lgT > 0 && ((1LL << lgT) > (long long)n2 * n3 ||
                        x_fused_smem(ns, n1, lgT, line_pitch(n1), vsize, bsize) > 110 * 1024))
       --lgT;
-    g.valid = table_tiles > 0 ? set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 1, false, false, table_tiles)
+    // tile table: a CTA per line pair, or per line when a pair's tile does not fit
+    g.valid = table_tiles > 0 ? (set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 1, false, false, table_tiles) ||
+                                 set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 0, false, false, table_tiles))
                               : set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
   }
   return g;

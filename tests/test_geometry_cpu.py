@@ -64,6 +64,24 @@ int main() {
         Geometry g = make_geometry(n1, n2, n3, ns, vs, bs, true);
         const bool expect_fit = x_fused_smem(ns, n1, 0, line_pitch(n1), vs, bs) <= kMaxDynSmem;
         CHECK(g.valid == expect_fit, "validity");
+        if (vs == 8 && bs == 4) {  // the FP32 stored-table form: mirrored tile table
+          const long long tiles = (long long)make_tile_table(n1, n2, n3, ns * (ns + 1) / 2, true).tiles.size();
+          Geometry t = make_geometry(n1, n2, n3, ns, vs, bs, true, tiles);
+          const bool fit = x_fused_smem(ns, n1, 0, line_pitch(n1), vs, bs, true) <= kMaxDynSmem;
+          CHECK(t.valid == fit && (!fit || (t.xTable && t.xLgT <= 1)), "table validity");
+          if (t.valid) {
+            CHECK(t.xTiles == (t.xLgT == 1 ? tiles : (long long)n2 * n3), "table tiles");
+            CHECK(t.xSmem == x_fused_smem(ns, n1, t.xLgT, t.xPitch, vs, bs, true), "table smem");
+            for (int lg = 0; lg <= 1; ++lg)
+              for (bool warp : {false, true}) {
+                Geometry h = t;
+                if (!set_x_geometry(h, n1, n2, n3, ns, vs, bs, lg, false, warp, tiles)) continue;
+                CHECK(h.xTable && h.xSmem <= kMaxDynSmem && h.xThreads % 32 == 0 && h.xThreads <= 384, "table x");
+                CHECK(h.xSmem == (warp ? xw_smem(ns, ilog2(n1), lg, bs, true)
+                                       : x_fused_smem(ns, n1, lg, h.xPitch, vs, bs, true)), "table x smem");
+              }
+          }
+        }
         if (!g.valid) continue;
         ++checked;
         z_ok(g, n1, n2, n3, ns, vs, bs); y_ok(g, n1, n2, n3, ns, vs, bs); x_ok(g, n1, n2, n3, ns, vs, bs);
