@@ -9,8 +9,7 @@ static cudaError_t zpass_lg(unsigned blocks, int threads, size_t smem, cudaStrea
   static SmemOptIn configured;
   cudaError_t e = ensure_smem(zpass_kernel<T, LG>, smem, configured);
   if (e != cudaSuccess) return e;
-  zpass_kernel<T, LG><<<blocks, threads, smem, st>>>(p);
-  return cudaGetLastError();
+  return launch_pdl(zpass_kernel<T, LG>, blocks, threads, smem, st, p);
 }
 
 template <typename T>
@@ -51,9 +50,8 @@ static cudaError_t strided_lg(unsigned blocks, int threads, size_t smem, cudaStr
   static SmemOptIn configured;
   cudaError_t e = ensure_smem(fft_strided_kernel<T, S, LG>, smem, configured);
   if (e != cudaSuccess) return e;
-  fft_strided_kernel<T, S, LG><<<blocks, threads, smem, st>>>(a.data, LG, a.lgTI, a.inner, a.tiles, a.tw, a.active,
-                                                             a.outer_per_rep, a.pitch);
-  return cudaGetLastError();
+  return launch_pdl(fft_strided_kernel<T, S, LG>, blocks, threads, smem, st, a.data, LG, a.lgTI, a.inner, a.tiles,
+                    a.tw, a.active, a.outer_per_rep, a.pitch);
 }
 
 template <typename T, int S>

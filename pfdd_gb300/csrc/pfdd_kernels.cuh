@@ -226,12 +226,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
     else
       bulk_copy(xs, xif + lb, (unsigned)nel * 16u, &xbar);
   }
-  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   // x-fastest layout with a forward transform that ends in the store: the S
   // lines go global <-> registers (consecutive lanes on consecutive x, so every
   // access covers whole TL-element runs), shared memory only between stages
   constexpr bool kIO = LG >= 3;
   const bool direct = kIO && xf && (p.flags & Z_FWD) && (p.flags & Z_STORE);
+  // S and the step counter come from the kernels before this one (and the
+  // FFT-boundary plans write their twiddles right before it); xi (the TMA
+  // copy above) from the z-pass before those, complete by then
+  griddep_wait();
+  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   if (p.flags & Z_SRC_XI) {
     for (int e = tid; e < nel; e += nthr)
       sm[sidx(e)] = from_xi<V>(xif[lb + (e >> lgL) * ls + (e & (L - 1))]);
@@ -350,6 +354,9 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
   if (active && !active[o / outer_per_rep]) return;
   V *base = reinterpret_cast<V *>(data_) + o * (long long)L * inner + c0;
   const int nel = L << lgTI, tid = threadIdx.x, nthr = blockDim.x;
+  // the lines come from the kernel before this one (and the FFT-boundary
+  // plans write their twiddles right before it)
+  griddep_wait();
   load_twiddles(tws, reinterpret_cast<const V *>(tw_), L);
   if constexpr (LG >= 3) {
     // lines straight from global memory into registers (consecutive lanes on
@@ -613,8 +620,7 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   // same B block run together, so it comes from HBM once and then from L2
   const long long r = blockIdx.x % p.R;
   const long long tile = blockIdx.x / p.R;
-  if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
-  if (p.active && !p.active[r]) return;
+  const bool idle = p.active && !p.active[r];
   const long long c0 = tile << lgT;
   const int npt = L << lgT;
   V *S = reinterpret_cast<V *>(p.S);
@@ -657,23 +663,29 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   const int fstride = (int)p.inner * L;
   auto goff = [&](int ln) { return (ln >> lgT) * fstride + cidx(ln & (TT - 1)) * L; };
   auto live = [&](int ln) { return (ln & (TT - 1)) < tl; };
+  // B tile: one contiguous block of bvals values, TMA bulk copies issued by
+  // one thread so it streams in during the forward FFT; B(k) and the
+  // twiddles are constant, so they load before the previous kernel is done
+  __shared__ __align__(8) uint64_t bbar;
+  const int bbytes = BFLY ? 0 : bvals * (int)sizeof(T);
+  const bool bulk = !BFLY && (bbytes & 15) == 0 && ((boff * (long long)sizeof(T)) & 15) == 0;
+  if (!idle) {
+    if (bulk && tid == 0) {
+      mbar_init(&bbar, 1);
+      bulk_load(Bs, Bt, (unsigned)bbytes, &bbar);
+    }
+    if (!BFLY && !bulk)
+      for (int i = tid; i < bvals; i += nthr) Bs[i] = Bt[i];
+    load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  }
+  griddep_wait();  // S and the step counter come from the kernels before this one
+  if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
+  if (idle) return;
   for (int e = tid; e < nel; e += nthr) {
     const int x = e & (L - 1), ln = e >> lgL;
     if (live(ln)) cp_async_elem(&sm[ln * LP + x], Sr + goff(ln) + x);
   }
   cp_async_commit();
-  // B tile: one contiguous block of bvals values, TMA bulk copies issued by
-  // one thread so it streams in during the forward FFT
-  __shared__ __align__(8) uint64_t bbar;
-  const int bbytes = BFLY ? 0 : bvals * (int)sizeof(T);
-  const bool bulk = !BFLY && (bbytes & 15) == 0 && ((boff * (long long)sizeof(T)) & 15) == 0;
-  if (bulk && tid == 0) {
-    mbar_init(&bbar, 1);
-    bulk_load(Bs, Bt, (unsigned)bbytes, &bbar);
-  }
-  if (!BFLY && !bulk)
-    for (int i = tid; i < bvals; i += nthr) Bs[i] = Bt[i];
-  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   cp_async_wait<0>();
   __syncthreads();
   for (int l0 = 0; l0 < lines; l0 += teams) {
@@ -754,8 +766,7 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   // same B block run together, so it comes from HBM once and then from L2
   const long long r = blockIdx.x % p.R;
   const long long tile = blockIdx.x / p.R;
-  if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
-  if (p.active && !p.active[r]) return;
+  const bool idle = p.active && !p.active[r];
   const long long c0 = tile << lgT;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
   const int th = lane & (LV - 1), wl = lane / LV;  // team thread, line of the warp
@@ -786,11 +797,17 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   const int fstride = (int)p.inner * L;
   auto goff = [&](int ln) { return (ln >> lgT) * fstride + cidx(ln & (TT - 1)) * L; };
   __shared__ __align__(8) uint64_t bbar;
-  if (!BFLY && tid == 0) {  // B tile: bvals contiguous values (a multiple of 16 bytes)
-    mbar_init(&bbar, 1);
-    bulk_load(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
+  // B(k) and the twiddles are constant: they load before the previous kernel is done
+  if (!idle) {
+    if (!BFLY && tid == 0) {  // B tile: bvals contiguous values (a multiple of 16 bytes)
+      mbar_init(&bbar, 1);
+      bulk_load(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
+    }
+    load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   }
-  load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
+  griddep_wait();  // S and the step counter come from the kernels before this one
+  if (p.step_ctr && blockIdx.x == 0 && threadIdx.x == 0) *p.step_ctr += 1;
+  if (idle) return;
   __syncthreads();  // twiddles (the second stage on) and the barrier's initialisation
   for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
     const int ln = ln0 + wl;

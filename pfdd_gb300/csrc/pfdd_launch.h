@@ -243,6 +243,25 @@ inline TileTable make_tile_table(int n1, int n2, int n3, int P, bool symmetric) 
   return t;
 }
 
+// Launches a step kernel with programmatic dependent launch allowed (see
+// griddep_wait): its CTAs may be scheduled while the previous kernel on the
+// stream finishes; the kernel orders its dependent reads itself.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned blocks, int threads, size_t smem, cudaStream_t st,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Per-kernel record of the dynamic shared memory opted into on each device.
 // Contexts on different host threads (the server's workers) launch the same
 // kernels concurrently, so updates are serialised and only ever raise it.

@@ -10,8 +10,7 @@ static cudaError_t launch_lg(unsigned blocks, int threads, size_t smem, cudaStre
   static SmemOptIn configured;
   cudaError_t e = ensure_smem(x_fused_kernel<float, NS, false, LG, true>, smem, configured);
   if (e != cudaSuccess) return e;
-  x_fused_kernel<float, NS, false, LG, true><<<blocks, threads, smem, st>>>(p);
-  return cudaGetLastError();
+  return launch_pdl(x_fused_kernel<float, NS, false, LG, true>, blocks, threads, smem, st, p);
 }
 
 template <int NS>

@@ -9,8 +9,7 @@ static cudaError_t launch_lg(unsigned blocks, int threads, size_t smem, cudaStre
   static SmemOptIn configured;
   cudaError_t e = ensure_smem(x_warp_kernel<NS, LG, BFLY>, smem, configured);
   if (e != cudaSuccess) return e;
-  x_warp_kernel<NS, LG, BFLY><<<blocks, threads, smem, st>>>(p);
-  return cudaGetLastError();
+  return launch_pdl(x_warp_kernel<NS, LG, BFLY>, blocks, threads, smem, st, p);
 }
 
 template <int NS, bool BFLY>

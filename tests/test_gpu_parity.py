@@ -303,3 +303,15 @@ def test_degenerate_and_long_axes_match_oracle(native_lib, n):
     assert rel(g64, go) <= GAMMA_RTOL
     x32, g32, _, _ = run_gpu(spec, "fp32")
     assert np.max(np.abs(x32 - xo)) <= 1e-5
+
+
+@pytest.mark.parametrize("n", [(512, 2, 4), (256, 4, 4), (8, 4, 2)])
+def test_fp32_table_form_twelve_systems_long_and_short_lines(native_lib, n):
+    """The FP32 stored-table form with 12 systems on 512-long x lines (the
+    line-pair tile does not fit: a CTA per line), 256-long ones, and lines
+    shorter than the warp-team range, against the FP64 oracle."""
+    spec = workloads.SolveSpec(n=n, ns=12, steps=8, sigma_max=0.04, noise_seed=14, noise_amp=0.05)
+    xo, go, _ = oracle.solve(spec)
+    x32, g32, _, _ = run_gpu(spec, "fp32")
+    assert np.max(np.abs(x32 - xo)) <= 1e-5
+    assert rel(g32, go) <= FP32_GAMMA_RTOL
