@@ -420,7 +420,7 @@ struct BLayout {
 __host__ __device__ __forceinline__ int b_mirror(int i, int n) { return (n - i) & (n - 1); }
 // row width of a mirrored tile (N1 values + the Nyquist column, a multiple of
 // 4 so every block is a whole number of 16-byte units)
-__host__ __device__ __forceinline__ int b_wm(int L) { return (L + 4) / 4 * 4; }
+__host__ __device__ constexpr int b_wm(int L) { return (L + 4) / 4 * 4; }
 // -1: not stored (the mirror's value, see BLayout)
 __host__ __device__ __forceinline__ long long b_index(const BLayout &bl, int p, long long pt) {
   const long long x = pt / bl.inner, c = pt - x * bl.inner;
@@ -477,9 +477,13 @@ __device__ __forceinline__ float frec_f(int i, int n, float d) {
 // ascending), with the point's B(k) in the shared-memory tile Bs: pair p's
 // value at Bs[p * W + bx].  at(a) is the point's value of field a (read, then
 // overwritten).  IN_REGS keeps the NS inputs in registers.
-template <typename T, int NS, bool IN_REGS, typename At>
-__device__ __forceinline__ void contract_table(const T *Bs, int W, int bx, At at) {
+// WC > 0: the row width is that compile-time W (the B loads then address off
+// one base register with immediate offsets).
+template <typename T, int NS, bool IN_REGS, int WC = 0, typename At>
+__device__ __forceinline__ void contract_table(const T *Bs, int Wrt, int bx, At at) {
   using V = typename cpx<T>::t;
+  const int W = WC > 0 ? WC : Wrt;
+  Bs += bx;
   V out[NS];
   V in[IN_REGS ? NS : 1];
 #pragma unroll
@@ -493,7 +497,7 @@ __device__ __forceinline__ void contract_table(const T *Bs, int W, int bx, At at
     const V ina = IN_REGS ? in[a] : at(a);
 #pragma unroll
     for (int b = a; b < NS; ++b, ++pidx) {
-      const T v = Bs[pidx * W + bx];
+      const T v = Bs[pidx * W];
       const V inb = IN_REGS ? in[b] : at(b);
       out[a].x += inb.x * v;
       out[a].y += inb.y * v;
@@ -826,13 +830,28 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   __syncthreads();
   for (int q = tid; q < (tl << LG); q += nthr) {
     const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
-    auto at = [&](int a) -> V & { return sm[(a * TT + t) * LP + sx]; };
+    V *const pt = sm + t * LP + sx;  // the point's value of field a at pt[a * T * LP]
     if constexpr (BFLY) {
-      contract_bfly<NS>(p.bf, at, x, L, c0 + t);
+      contract_bfly<NS>(p.bf, [&](int a) -> V & { return pt[a * TT * LP]; }, x, L, c0 + t);
     } else {
       const int role = lgT == 0 ? role0 : t;
       const int bx = !tabled ? q : (role == 0 ? x : (x == L / 2 ? L : b_mirror(x, L)));
-      contract_table<float, NS, true>(Bs, W, bx, at);
+      // the table form's row widths (a mirrored pair, a single line) and tile
+      // widths (T = 1, 2) as constants: every shared-memory access of the
+      // contraction is an immediate offset from pt or from the B row
+      auto table = [&](auto wc, auto tc) {
+        constexpr int WC = decltype(wc)::value, TC = decltype(tc)::value;
+        contract_table<float, NS, true, WC>(Bs, W, bx, [&](int a) -> V & { return pt[a * TC * LP]; });
+      };
+      using I = std::integral_constant<int, 1>;
+      using II = std::integral_constant<int, 2>;
+      using WM = std::integral_constant<int, b_wm(L)>;
+      using WS = std::integral_constant<int, L>;
+      if (tabled && mirrored && lgT == 1) table(WM{}, II{});
+      else if (tabled && mirrored && lgT == 0) table(WM{}, I{});
+      else if (tabled && W == L && lgT == 1) table(WS{}, II{});
+      else if (tabled && W == L && lgT == 0) table(WS{}, I{});
+      else contract_table<float, NS, true>(Bs, W, bx, [&](int a) -> V & { return pt[a * TT * LP]; });
     }
   }
   __syncthreads();
