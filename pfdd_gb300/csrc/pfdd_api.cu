@@ -26,8 +26,6 @@
 
 namespace pfdd {
 
-// Deterministic second stage of the gamma sums: one block per (step, replica),
-// fixed-shape tree over the partials of each system.
 __global__ void fill_u64_kernel(unsigned long long *p, long long n, unsigned long long v) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     p[i] = v;
@@ -43,37 +41,60 @@ __device__ __forceinline__ double i128_to_double(__int128 v) {
   return neg ? -d : d;
 }
 
-__global__ void __launch_bounds__(256) gamma_reduce_kernel(const long long *part, int nparts, int R, int ns,
-                                                           double scale, double *gamma_a, double *gamma) {
-  __shared__ __int128 red[256];
+// Second stage of the gamma sums: a block per (step, replica), kGammaWarps
+// warps per system (block of kGammaWarps * 32 * ns threads).  The sums are
+// exact integers, so neither the split of the partials over lanes nor the
+// order of the additions changes a result.
+constexpr int kGammaWarps = 2;
+
+__device__ __forceinline__ __int128 shfl_down_i128(__int128 v, int o) {
+  const unsigned long long lo = __shfl_down_sync(0xffffffffu, (unsigned long long)v, o);
+  const long long hi = __shfl_down_sync(0xffffffffu, (long long)(v >> 64), o);
+  return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+
+__global__ void __launch_bounds__(kGammaWarps * 32 * kMaxNs) gamma_reduce_kernel(const long long *part, int nparts,
+                                                                                int R, int ns, double scale,
+                                                                                double *gamma_a, double *gamma) {
+  __shared__ __int128 red[kGammaWarps * kMaxNs];
+  __shared__ int redbad[kGammaWarps * kMaxNs];
   const int s = blockIdx.x / R, r = blockIdx.x - s * R;
-  __int128 tot = 0;
-  int totbad = 0;
-  for (int a = 0; a < ns; ++a) {
-    const long long *pp = part + ((long long)s * R * ns + (long long)r * ns + a) * nparts;
-    __int128 acc = 0;
-    int bad = 0;
-    for (int c = threadIdx.x; c < nparts; c += blockDim.x) {
-      const long long v = pp[c];
-      if (v == LLONG_MIN) bad = 1;
-      else acc += v;
-    }
-    red[threadIdx.x] = acc;
-    bad = __syncthreads_or(bad);
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      gamma_a[((long long)s * R + r) * ns + a] = bad ? __longlong_as_double(0x7ff8000000000000ll)
-                                                     : i128_to_double(red[0]) * scale;
-      tot += red[0];
-      totbad |= bad;
-    }
-    __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = w / kGammaWarps, part0 = (w % kGammaWarps) * 32 + lane;
+  const long long *pp = part + ((long long)s * R * ns + (long long)r * ns + a) * nparts;
+  __int128 acc = 0;
+  int bad = 0;
+#pragma unroll 8
+  for (int c = part0; c < nparts; c += kGammaWarps * 32) {
+    const long long v = pp[c];
+    bad |= v == LLONG_MIN;
+    acc += v == LLONG_MIN ? 0 : v;
   }
-  if (threadIdx.x == 0)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += shfl_down_i128(acc, o);
+  bad = __any_sync(0xffffffffu, bad);
+  if (lane == 0) {
+    red[w] = acc;
+    redbad[w] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __int128 tot = 0;
+    int totbad = 0;
+    for (int b = 0; b < ns; ++b) {
+      __int128 sa = 0;
+      int ba = 0;
+      for (int k = 0; k < kGammaWarps; ++k) {
+        sa += red[b * kGammaWarps + k];
+        ba |= redbad[b * kGammaWarps + k];
+      }
+      gamma_a[((long long)s * R + r) * ns + b] = ba ? __longlong_as_double(0x7ff8000000000000ll)
+                                                    : i128_to_double(sa) * scale;
+      tot += sa;
+      totbad |= ba;
+    }
     gamma[blockIdx.x] = totbad ? __longlong_as_double(0x7ff8000000000000ll) : i128_to_double(tot) * scale;
+  }
 }
 
 // ---- strain and stress fields (diagnostics) --------------------------------
@@ -1226,8 +1247,8 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
     }
     const int nt = ks * c->nrep;
     t_begin(c);
-    gamma_reduce_kernel<<<nt, kThreads, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns, 0x1p-44 * zp.inv_n,
-                                                    c->gam_a, c->gam);
+    gamma_reduce_kernel<<<nt, kGammaWarps * 32 * c->ns, 0, c->st>>>(c->part, c->g.zNparts, c->nrep, c->ns,
+                                                                   0x1p-44 * zp.inv_n, c->gam_a, c->gam);
     t_end(c, K_GAMMA);
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(c->h_gam_a, c->gam_a, (size_t)ks * RF * sizeof(double), cudaMemcpyDeviceToHost, c->st));
