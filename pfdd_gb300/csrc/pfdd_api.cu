@@ -376,6 +376,10 @@ struct pfdd_ctx {
   int *xline = nullptr, *xord = nullptr;
   long long ntiles = 0, bvals = 0;
   bool xtSym = true;
+  // the step's y passes take the fields from the last down: the z-pass runs
+  // them upwards, so each y pass starts on the fields that the pass before it
+  // wrote last, which are still in L2 (the x-pass takes every field per tile)
+  bool yRev = true;
   BFlyParams bf{};
   long long launches = 0;
   KTiming tm;
@@ -919,7 +923,7 @@ static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/) {
   t_begin(c);
   cudaError_t e = launch_strided(prec_code(c->prec), sign, ilog2(L), (unsigned)blocks, c->g.threads[gi], c->g.smem[gi],
                                  c->st, c->S, c->g.lgTI[gi], inner, c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0],
-                                 c->active, outer_per_rep, c->g.pitch[gi]);
+                                 c->active, outer_per_rep, c->g.pitch[gi], ax == 0 && c->yRev);
   t_end(c, ax == 0 ? (sign < 0 ? K_FFT_Y_FWD : K_FFT_Y_INV) : (sign < 0 ? K_FFT_X_FWD : K_FFT_X_INV));
   return e;
 }
@@ -1021,16 +1025,19 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,x=<tile columns>,w=<0|1>,y=<tile columns>" pins the
-  // plan (each entry optional, ignored when it does not fit; w=1, the
-  // warp-team x-pass, after x) instead of timing it, e.g. to profile the plan a
-  // timed run chose (a profiler distorts the timings)
+  // PFDD_PLAN="z=<lines>,x=<tile columns>,w=<0|1>,y=<tile columns>,f=<0|1>"
+  // pins the plan (each entry optional, ignored when it does not fit; w=1, the
+  // warp-team x-pass, after x; f=0, the y passes in ascending field order)
+  // instead of timing it, e.g. to profile the plan a timed run chose (a
+  // profiler distorts the timings)
   if (const char *pin = std::getenv("PFDD_PLAN")) {
     const size_t vs = vsize_of(c->prec), bs = bsize_of(c->prec);
     for (const char *q = pin; *q;) {
       char key = 0;
       int v = 0;
-      if (std::sscanf(q, "%c=%d", &key, &v) == 2 && v > 0) {
+      const bool kv = std::sscanf(q, "%c=%d", &key, &v) == 2;
+      if (kv && key == 'f') c->yRev = v != 0;
+      if (kv && v > 0) {
         Geometry g = c->g;
         const long long tt = uses_tile_table(c->prec) ? c->ntiles : 0;
         const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v) && g.zNparts <= c->zparts_cap

@@ -42,7 +42,7 @@ struct StridedArgs {
   const void *tw;
   const uint8_t *active;
   long long outer_per_rep;
-  int pitch;
+  int pitch, rev;
 };
 
 template <typename T, int S, int LG>
@@ -51,7 +51,7 @@ static cudaError_t strided_lg(unsigned blocks, int threads, size_t smem, cudaStr
   cudaError_t e = ensure_smem(fft_strided_kernel<T, S, LG>, smem, configured);
   if (e != cudaSuccess) return e;
   return launch_pdl(fft_strided_kernel<T, S, LG>, blocks, threads, smem, st, a.data, LG, a.lgTI, a.inner, a.tiles,
-                    a.tw, a.active, a.outer_per_rep, a.pitch);
+                    a.tw, a.active, a.outer_per_rep, a.pitch, a.rev);
 }
 
 template <typename T, int S>
@@ -74,8 +74,8 @@ static cudaError_t strided_t(int lgL, unsigned blocks, int threads, size_t smem,
 
 cudaError_t launch_strided(int prec, int sign, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                            void *data, int lgTI, long long inner, long long tiles_per_outer, const void *tw,
-                           const uint8_t *active, long long outer_per_rep, int pitch) {
-  const StridedArgs a{data, lgTI, inner, tiles_per_outer, tw, active, outer_per_rep, pitch};
+                           const uint8_t *active, long long outer_per_rep, int pitch, bool rev) {
+  const StridedArgs a{data, lgTI, inner, tiles_per_outer, tw, active, outer_per_rep, pitch, rev ? 1 : 0};
   if (prec == 0)
     return sign < 0 ? strided_t<double, -1>(lgL, blocks, threads, smem, st, a)
                     : strided_t<double, +1>(lgL, blocks, threads, smem, st, a);

@@ -343,14 +343,17 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
 template <typename T, int S, int LG>
 __global__ void __launch_bounds__(256)
 fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long tiles_per_outer, const void *tw_,
-                   const uint8_t *active, long long outer_per_rep, int pitch) {
+                   const uint8_t *active, long long outer_per_rep, int pitch, int rev) {
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int L = 1 << lgL, TI = 1 << lgTI;
   V *tws = reinterpret_cast<V *>(smraw);
   V *sm = tws + L;
-  const long long o = blockIdx.x / tiles_per_outer;
-  const long long c0 = (blockIdx.x - o * tiles_per_outer) << lgTI;
+  // rev: the outer index (field) runs from the last down, so that the first
+  // blocks take the fields the previous pass wrote last (still in L2)
+  const long long ob = blockIdx.x / tiles_per_outer;
+  const long long o = rev ? (long long)gridDim.x / tiles_per_outer - 1 - ob : ob;
+  const long long c0 = (blockIdx.x - ob * tiles_per_outer) << lgTI;
   if (active && !active[o / outer_per_rep]) return;
   V *base = reinterpret_cast<V *>(data_) + o * (long long)L * inner + c0;
   const int nel = L << lgTI, tid = threadIdx.x, nthr = blockDim.x;
@@ -805,7 +808,7 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   if (!idle) {
     if (!BFLY && tid == 0) {  // B tile: bvals contiguous values (a multiple of 16 bytes)
       mbar_init(&bbar, 1);
-      bulk_load(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
+      bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
     }
     load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   }

@@ -19,7 +19,7 @@ cudaError_t launch_zpass(int prec, int lgL, unsigned blocks, int threads, size_t
 // strided line FFT (sign -1 forward, +1 inverse) for lgL in [0, 9]
 cudaError_t launch_strided(int prec, int sign, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                            void *data, int lgTI, long long inner, long long tiles_per_outer, const void *tw,
-                           const uint8_t *active, long long outer_per_rep, int pitch);
+                           const uint8_t *active, long long outer_per_rep, int pitch, bool rev = false);
 // fused x-pass (x-forward FFT, contraction, x-inverse FFT) for ns in [1, 12]
 cudaError_t launch_x_fused_f32(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p);
 cudaError_t launch_x_fused_f64(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p);

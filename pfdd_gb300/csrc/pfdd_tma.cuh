@@ -86,6 +86,22 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
   }
 }
 
+// The same with an L2 evict-first policy: for data read once (a B(k) tile),
+// so that it does not push out of L2 what the previous pass wrote last.
+__device__ __forceinline__ void bulk_load_evict_first(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  mbar_arrive_expect_tx(bar, bytes);
+  for (unsigned off = 0; off < bytes; off += kBulkChunk) {
+    const unsigned n = bytes - off < kBulkChunk ? bytes - off : kBulkChunk;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_u32((const char *)dst + off)),
+        "l"((const char *)src + off), "r"(n), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+  }
+}
+
 // Programmatic dependent launch (kernels launched with launch_pdl): a kernel
 // may be launched while the previous kernel on its stream finishes, does the
 // work that does not depend on it (constant tables, TMA copies of data written

@@ -156,3 +156,17 @@ def test_table_form_line_and_pair_ctas_same_bits(native_lib, n, plan):
     assert p1["x_pass"]["b_mirrored"] == p2["x_pass"]["b_mirrored"] == 1
     np.testing.assert_array_equal(g1, g2)
     np.testing.assert_array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_y_field_order_same_bits(native_lib, precision):
+    """The step's y passes take the fields from the last down (so each starts
+    on what the pass before it wrote last); the ascending order (f=0) gives the
+    same bits, one solve and a batch."""
+    spec = workloads.SolveSpec(n=(32, 16, 8), ns=5, steps=6, sigma_max=0.05, noise_seed=36,
+                               loops=workloads.random_loops((32, 16, 8), 2, 1.0, 3.0, 5, seed=36))
+    for nrep in (1, 3):
+        g1, x1, _ = pinned(spec, precision, "f=1", nrep=nrep)
+        g0, x0, _ = pinned(spec, precision, "f=0", nrep=nrep)
+        np.testing.assert_array_equal(g1, g0)
+        np.testing.assert_array_equal(x1, x0)
