@@ -349,11 +349,11 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
   const int L = 1 << lgL, TI = 1 << lgTI;
   V *tws = reinterpret_cast<V *>(smraw);
   V *sm = tws + L;
-  // rev: the outer index (field) runs from the last down, so that the first
-  // blocks take the fields the previous pass wrote last (still in L2)
-  const long long ob = blockIdx.x / tiles_per_outer;
-  const long long o = rev ? (long long)gridDim.x / tiles_per_outer - 1 - ob : ob;
-  const long long c0 = (blockIdx.x - ob * tiles_per_outer) << lgTI;
+  // rev: the blocks run from the last down, so that the first take the
+  // fields the previous pass wrote last (still in L2)
+  const long long bid = rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+  const long long o = bid / tiles_per_outer;
+  const long long c0 = (bid - o * tiles_per_outer) << lgTI;
   if (active && !active[o / outer_per_rep]) return;
   V *base = reinterpret_cast<V *>(data_) + o * (long long)L * inner + c0;
   const int nel = L << lgTI, tid = threadIdx.x, nthr = blockDim.x;
