@@ -164,7 +164,7 @@ __device__ __forceinline__ long long update_tile_f32(const ZParams &p, const Upd
                                                       __longlong_as_double((long long)f32_to_f64bits_fast(dre)));
       xb.y = (unsigned long long)__double_as_longlong(__longlong_as_double((long long)xb.y) -
                                                       __longlong_as_double((long long)f32_to_f64bits_fast(dim)));
-      xg[pt] = xb;
+      __stcs(&xg[pt], xb);  // read again only by the next step's z-pass: evict first
     }
     acc += to_fixed_bits(xb.x, big);
     float2 o;
