@@ -315,3 +315,28 @@ def test_fp32_table_form_twelve_systems_long_and_short_lines(native_lib, n):
     x32, g32, _, _ = run_gpu(spec, "fp32")
     assert np.max(np.abs(x32 - xo)) <= 1e-5
     assert rel(g32, go) <= FP32_GAMMA_RTOL
+
+
+@pytest.mark.parametrize("ns", [1, 2, 7])
+def test_small_and_odd_system_counts_match_oracle(native_lib, ns):
+    """Slip-system counts away from 3 and 12 (every count has its own compiled
+    x-pass, and the gamma reduction sizes its block by it), all three forms,
+    with a pinned point, against the FP64 oracle."""
+    n = (32, 8, 16)
+    spec = workloads.SolveSpec(n=n, ns=ns, steps=10, sigma_max=0.05, noise_seed=40 + ns,
+                               loops=workloads.random_loops(n, 2, 1.5, 3.0, ns, seed=40 + ns))
+    x0, b0 = workloads.initial_state(spec)
+    bc = b0.copy()
+    bc[0, 3, 2, 1] = 1.0  # one pinned point
+    eps = oracle.fcc_eps(ns, bdiv=float(np.sqrt(2.0)), dslip=np.full(12, spec.dslip))
+    B = oracle.bmatrix(spec.n, eps, 2.0 * spec.mu + spec.lam, spec.lam, spec.mu, spec.d)
+    xo, go, gao = oracle.run(spec.n, B, x0, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf),
+                             np.full(ns, spec.dslip), 1.0, native.spec_tau(spec))
+    x64, g64, ga64, _ = run_gpu(spec, "fp64", bc=bc)
+    assert np.max(np.abs(x64 - xo)) <= XI_TOL
+    assert rel(g64, go) <= GAMMA_RTOL
+    assert np.max(np.abs(ga64 - gao)) <= GAMMA_RTOL * max(1e-3, np.max(np.abs(gao)))
+    for form in ("fp32", "fp32_bfly"):
+        x32, g32, _, _ = run_gpu(spec, form, bc=bc)
+        assert np.max(np.abs(x32 - xo)) <= 1e-5
+        assert rel(g32, go) <= FP32_GAMMA_RTOL
