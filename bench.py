@@ -603,7 +603,8 @@ def run_ours(a):
                    "l2": "inputs larger than L2 (xi 403 MB + S 201 MB per step"
                          + ("" if head == "fp32_bfly" else
                             f" + B(k) table {b_table_bytes(head, spec.n, spec.ns, rh['plan']) / 1e6:.0f} MB")
-                         + ", L2 126 MB)"},
+                         + ", L2 126 MB; within a step each pass starts on the fields the previous pass"
+                         " left in L2, by the order of its blocks)"},
         "updates_per_s": round(vh * spec.npts * spec.ns, 1),
         "hbm_roofline_step": {"algorithmic_bytes_per_step": step_bytes,
                               "achieved_gbs": round(step_bytes * vh / dist.world / 1e9, 1),
