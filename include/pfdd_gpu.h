@@ -199,13 +199,21 @@ pfdd_status pfdd_fft_backward(pfdd_fft_plan *plan, void *data, int batch, int on
  * process held to a fixed device-memory budget.  Its only scratch, the twiddle
  * tables, is one static device array in the library (24 KB, held by every GPU
  * that loads the library until the process exits), so N1, N2, N3 are limited
- * to powers of two <= 512: larger sizes return PFDD_ELIMIT, other invalid
- * arguments PFDD_EINVAL.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls
- * share the array and each rewrites it before use, so calls that overlap on
- * the GPU (different streams, or different threads) race: serialise them.
- * The call returns after enqueueing; synchronise `stream` before reading
- * `data`. */
+ * to powers of two <= 512: larger sizes return PFDD_ELIMIT, a batch whose
+ * launch grids would exceed 2^31 - 1 blocks and other invalid arguments
+ * PFDD_EINVAL.  The first call on a device looks up the array's device
+ * address (again whenever the current CUDA context is not the one it was
+ * looked up in); make that first call before any stream capture.  The cached
+ * address does not survive cudaDeviceReset: do not reset a device between
+ * calls of a process that uses this entry point.  Under CUDA's
+ * default lazy module loading the first call on a device, and the first call
+ * of each new line length, may load kernel code, which takes device memory:
+ * make those calls once at set-up (or set CUDA_MODULE_LOADING=EAGER) if the
+ * budget leaves no room for that later.  All calls share the array and each
+ * rewrites it before use, so calls that overlap on the GPU (different
+ * streams, or different threads) race: serialise them.  Calls queued one
+ * after another on one stream are ordered.  The call returns after
+ * enqueueing; synchronise `stream` before reading `data`. */
 pfdd_status pfdd_fft_device_noalloc(void *data, int n1, int n2, int n3, int batch, int precision, int sign,
                                     void *stream);
 

@@ -53,7 +53,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
-REF_SRC = Path("/root/reference/PFDD_Final_GPU.c")
+# the reference checkout: $PFDD_REFERENCE_DIR, else a checkout named `reference`
+# beside this repository's parent directory
+REF_ROOT = Path(os.environ.get("PFDD_REFERENCE_DIR", str(HERE.parents[1] / "reference")))
+REF_SRC = REF_ROOT / "PFDD_Final_GPU.c"
 PATCHED = REF_DIR / "pfdd_ref_patched.c"
 
 DEFAULTS_BLOCK = r"""
@@ -229,10 +232,14 @@ def bench_variants():
             dict(n=(128, 128, 128), k=1000, sigma=0.05, fp64=True, diag=False, setup_b=False)]
 
 
-def run_ref(binary: Path, workdir: Path, timeout=None, quiet=True):
-    """Run a patched-reference binary in ``workdir`` (which must hold xi.dat and xi_bc.dat)."""
+def run_ref(binary: Path, workdir: Path, timeout=None, quiet=True, krun: int | None = None):
+    """Run a patched-reference binary in ``workdir`` (which must hold xi.dat and xi_bc.dat).
+    krun: run only the first ``krun`` steps of the K-step ramp (patch 4)."""
+    env = dict(os.environ)
+    if krun is not None:
+        env["PFDD_KRUN"] = str(int(krun))
     with open(workdir / "stdout.log", "w") as fo:
-        subprocess.run([str(binary)], cwd=workdir, check=True, timeout=timeout,
+        subprocess.run([str(binary)], cwd=workdir, check=True, timeout=timeout, env=env,
                        stdout=fo if quiet else None, stderr=subprocess.STDOUT)
 
 

@@ -400,7 +400,18 @@ struct pfdd_ctx {
   bool tuned = false, tune = true;
   int zparts_cap = 0;  // z-pass blocks per field the partial buffer holds
   std::string plan;  // the autotune record of the plan (JSON), reported with the current geometry
+  // failure tests, set from the host environment (0 in normal runs):
+  // PFDD_TEST_DROP_BULK=1 makes the x-pass's first CTA wait for B-tile bytes
+  // that are never copied (its bounded wait runs out: pfdd_step returns
+  // PFDD_ETIMEOUT); PFDD_TEST_FAIL_ALLOC=k makes the k-th device or pinned
+  // allocation of pfdd_create fail (PFDD_ENOMEM)
+  int drop_bulk = 0;
+  int alloc_count = 0, fail_alloc_at = 0;
 };
+
+// wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
+// limit is kWaitNs)
+constexpr unsigned long long kTestWaitNs = 2ull * 1000 * 1000;
 
 struct pfdd_fft_plan {
   int n[3] = {0, 0, 0};
@@ -559,6 +570,29 @@ static pfdd_status set_tile_layout(pfdd_ctx *c, bool symmetric) {
   return PFDD_OK;
 }
 
+// Device and pinned allocations of a context, counted so a failure test can
+// make the k-th one fail (PFDD_TEST_FAIL_ALLOC=k) as an exhausted device would.
+static cudaError_t ctx_malloc(pfdd_ctx *c, void **p, size_t bytes) {
+  if (c->fail_alloc_at > 0 && ++c->alloc_count == c->fail_alloc_at) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+static cudaError_t ctx_malloc_host(pfdd_ctx *c, void **p, size_t bytes) {
+  if (c->fail_alloc_at > 0 && ++c->alloc_count == c->fail_alloc_at) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocHost(p, bytes);
+}
+template <typename P> static cudaError_t ctx_malloc(pfdd_ctx *c, P **p, size_t bytes) {
+  return ctx_malloc(c, reinterpret_cast<void **>(p), bytes);
+}
+template <typename P> static cudaError_t ctx_malloc_host(pfdd_ctx *c, P **p, size_t bytes) {
+  return ctx_malloc_host(c, reinterpret_cast<void **>(p), bytes);
+}
+
 extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n3, int ns, int nrep, int precision,
                                            int device) {
   if (!out) return PFDD_EINVAL;
@@ -571,6 +605,7 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   c->n[0] = n1; c->n[1] = n2; c->n[2] = n3;
   c->ns = ns; c->nrep = nrep; c->prec = precision; c->dev = device;
   c->N = (long long)n1 * n2 * n3;
+  if (const char *v = std::getenv("PFDD_TEST_FAIL_ALLOC")) c->fail_alloc_at = std::atoi(v);
   CK(c, cudaSetDevice(device));
   CK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   TileTable tt;
@@ -584,39 +619,39 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
                 "pfdd_create: one x-line tile of %d systems x N1=%d with its B(k) does not fit in shared memory in "
                 "this precision", ns, n1);
   const size_t RF = (size_t)nrep * ns, N = (size_t)c->N, P = (size_t)ns * (ns + 1) / 2;
-  CK(c, cudaMalloc(&c->xi, RF * N * sizeof(double2)));
-  CK(c, cudaMalloc(&c->S, RF * N * vsize_of(precision)));
+  CK(c, ctx_malloc(c, &c->xi, RF * N * sizeof(double2)));
+  CK(c, ctx_malloc(c, &c->S, RF * N * vsize_of(precision)));
   c->bvals = (long long)b_values(n1, n2, n3, ns, precision);
-  if (c->bvals) CK(c, cudaMalloc(&c->B, (size_t)c->bvals * bsize_of(precision)));
+  if (c->bvals) CK(c, ctx_malloc(c, &c->B, (size_t)c->bvals * bsize_of(precision)));
   if (uses_tile_table(precision)) {
     const size_t inner = (size_t)n2 * n3;
-    CK(c, cudaMalloc(&c->xt, inner * sizeof(int2)));
-    CK(c, cudaMalloc(&c->xtoff, (inner + 1) * sizeof(long long)));
-    CK(c, cudaMalloc(&c->xline, inner * sizeof(int)));
-    CK(c, cudaMalloc(&c->xord, inner * sizeof(int)));
+    CK(c, ctx_malloc(c, &c->xt, inner * sizeof(int2)));
+    CK(c, ctx_malloc(c, &c->xtoff, (inner + 1) * sizeof(long long)));
+    CK(c, ctx_malloc(c, &c->xline, inner * sizeof(int)));
+    CK(c, ctx_malloc(c, &c->xord, inner * sizeof(int)));
     CK(c, upload_tile_table(c, tt));
   }
-  CK(c, cudaMalloc(&c->active, nrep));
-  CK(c, cudaMalloc(&c->dslip_dev, kMaxNs * sizeof(double)));
-  CK(c, cudaMalloc(&c->flag, sizeof(int)));
-  CK(c, cudaMalloc(&c->errflag, sizeof(int)));
-  CK(c, cudaMalloc(&c->step_ctr, sizeof(int)));
+  CK(c, ctx_malloc(c, &c->active, nrep));
+  CK(c, ctx_malloc(c, &c->dslip_dev, kMaxNs * sizeof(double)));
+  CK(c, ctx_malloc(c, &c->flag, sizeof(int)));
+  CK(c, ctx_malloc(c, &c->errflag, sizeof(int)));
+  CK(c, ctx_malloc(c, &c->step_ctr, sizeof(int)));
   if (const char *g = std::getenv("PFDD_NO_GRAPHS")) c->use_graphs = g[0] == '\0' || g[0] == '0';
   if (const char *g = std::getenv("PFDD_NO_TUNE")) c->tune = g[0] == '\0' || g[0] == '0';
   CK(c, cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st));
-  CK(c, cudaMallocHost(&c->h_errflag, sizeof(int)));
+  CK(c, ctx_malloc_host(c, &c->h_errflag, sizeof(int)));
   // partial sums for a chunk of steps, bounded to ~32 MB; sized for the
   // smallest z-pass block the autotuner may pick (a quarter of the default)
   c->zparts_cap = (int)std::min<long long>((long long)n1 * n2, (long long)c->g.zNparts * 4);
   const size_t per_step = RF * (size_t)c->zparts_cap;
   c->kchunk = (int)std::max<size_t>(1, std::min<size_t>(1024, (4u << 20) / per_step));
-  CK(c, cudaMalloc(&c->part, per_step * c->kchunk * sizeof(long long)));
-  CK(c, cudaMalloc(&c->tau, (size_t)c->kchunk * RF * sizeof(double)));
-  CK(c, cudaMalloc(&c->gam_a, (size_t)c->kchunk * RF * sizeof(double)));
-  CK(c, cudaMalloc(&c->gam, (size_t)c->kchunk * nrep * sizeof(double)));
-  CK(c, cudaMallocHost(&c->h_gam_a, (size_t)c->kchunk * RF * sizeof(double)));
-  CK(c, cudaMallocHost(&c->h_gam, (size_t)c->kchunk * nrep * sizeof(double)));
-  CK(c, cudaMallocHost(&c->h_tau, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, ctx_malloc(c, &c->part, per_step * c->kchunk * sizeof(long long)));
+  CK(c, ctx_malloc(c, &c->tau, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, ctx_malloc(c, &c->gam_a, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, ctx_malloc(c, &c->gam, (size_t)c->kchunk * nrep * sizeof(double)));
+  CK(c, ctx_malloc_host(c, &c->h_gam_a, (size_t)c->kchunk * RF * sizeof(double)));
+  CK(c, ctx_malloc_host(c, &c->h_gam, (size_t)c->kchunk * nrep * sizeof(double)));
+  CK(c, ctx_malloc_host(c, &c->h_tau, (size_t)c->kchunk * RF * sizeof(double)));
   CK(c, make_twiddles(c->tw, c->n, precision, c->st));
   c->h_active.assign(nrep, 1);
   CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), nrep, cudaMemcpyHostToDevice, c->st));
@@ -943,6 +978,8 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   t_begin(c);
   xp.bf = c->bf;
   xp.err = c->errflag;
+  xp.drop_bulk = c->drop_bulk;
+  xp.wait_ns = c->drop_bulk ? kTestWaitNs : kWaitNs;
   cudaError_t e = c->g.xWarp
                       ? launch_x_warp_f32(c->ns, c->prec == PFDD_FFT_FP32_BFLY, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
                   : c->prec == PFDD_FFT_FP32_BFLY
@@ -1286,6 +1323,14 @@ extern "C" pfdd_status pfdd_step(pfdd_ctx *c, int nsteps, const double *tau, dou
   if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_step: state not set");
   c->launches = 0;
   if (nsteps == 0) return PFDD_OK;
+  {
+    const char *v = std::getenv("PFDD_TEST_DROP_BULK");
+    const int want = v && v[0] && v[0] != '0';
+    if (want != c->drop_bulk) {
+      c->drop_bulk = want;
+      c->gen++;  // captured x-pass arguments
+    }
+  }
   CK(c, cudaSetDevice(c->dev));
   return c->prec == PFDD_FP64 ? run_steps<double>(c, nsteps, tau, gamma, gamma_a)
                               : run_steps<float>(c, nsteps, tau, gamma, gamma_a);

@@ -465,6 +465,11 @@ struct XParams {
   int L, lgL, lgT, pitch, R;
   int *err;                // set when a bounded wait times out (may be null)
   int *step_ctr;           // incremented once per launch (null: none); the z-pass reads it
+  // failure test (0 in normal runs): CTA 0 announces its B tile's bytes on the
+  // mbarrier but issues no copy, so its bounded wait (limit wait_ns) runs out;
+  // nothing is left in flight
+  int drop_bulk;
+  unsigned long long wait_ns;
   BFlyParams bf;
 };
 
@@ -679,7 +684,8 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
   if (!idle) {
     if (bulk && tid == 0) {
       mbar_init(&bbar, 1);
-      bulk_load(Bs, Bt, (unsigned)bbytes, &bbar);
+      if (p.drop_bulk && blockIdx.x == 0) mbar_arrive_expect_tx(&bbar, (unsigned)bbytes);
+      else bulk_load(Bs, Bt, (unsigned)bbytes, &bbar);
     }
     if (!BFLY && !bulk)
       for (int i = tid; i < bvals; i += nthr) Bs[i] = Bt[i];
@@ -699,7 +705,7 @@ __global__ void __launch_bounds__((IN_REGS || BFLY) ? 384 : 256, 2) x_fused_kern
     const int ln = l0 + my_team, a = ln >> lgT, t = ln & (TT - 1);
     line_fft<-1, LG, NV>(th, lgL, tws, [&](int l) { return &sm[sidx(a, t, l)]; }, ln < lines && live(ln));
   }
-  if (bulk) mbar_wait(&bbar, 0, p.err);
+  if (bulk) mbar_wait(&bbar, 0, p.err, p.wait_ns);
   __syncthreads();
   for (int q = tid; q < (tl << lgL); q += nthr) {
     const int t = q >> lgL, x = q & (L - 1);
@@ -808,7 +814,8 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   if (!idle) {
     if (!BFLY && tid == 0) {  // B tile: bvals contiguous values (a multiple of 16 bytes)
       mbar_init(&bbar, 1);
-      bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
+      if (p.drop_bulk && blockIdx.x == 0) mbar_arrive_expect_tx(&bbar, (unsigned)(bvals * 4));
+      else bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
     }
     load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   }
@@ -829,7 +836,7 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
     line_fft_io<-1, LG, true, false, NV, true>(v, th, tws, [&](int l) { return &line[xw_swz(l, LG)]; },
                                                [&](int l) { return &line[xw_swz(l, LG)]; }, act);
   }
-  if (!BFLY) mbar_wait(&bbar, 0, p.err);
+  if (!BFLY) mbar_wait(&bbar, 0, p.err, p.wait_ns);
   __syncthreads();
   for (int q = tid; q < (tl << LG); q += nthr) {
     const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);

@@ -9,6 +9,7 @@
 // within a device-memory budget fixed by someone else.  This entry point works
 // on the caller's device buffer in place and keeps its only scratch -- the
 // twiddle tables of the three axes -- in a file-scope static device array.
+#include <climits>
 #include <cstring>
 #include <mutex>
 
@@ -25,20 +26,51 @@ constexpr int kNoAllocMaxDevices = 64;
 __device__ __align__(256) unsigned char g_noalloc_twiddles[3 * kNoAllocMaxLen * 16];
 
 std::mutex g_noalloc_mu;
-void *g_noalloc_addr[kNoAllocMaxDevices] = {};
+// the array's device address per device, with the CUDA context it belongs to
+struct ScratchSlot {
+  void *ctx = nullptr;
+  void *addr = nullptr;
+};
+ScratchSlot g_noalloc_slot[kNoAllocMaxDevices];
+
+// cuCtxGetCurrent through the runtime's driver entry point (no link to the
+// driver library): the context current on this thread, null if none yet.
+cudaError_t current_context(void **ctx) {
+  using Fn = int (*)(void **);
+  static Fn fn = nullptr;  // resolved under g_noalloc_mu
+  if (!fn) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !f) return cudaErrorNotSupported;
+    fn = reinterpret_cast<Fn>(f);
+  }
+  *ctx = nullptr;
+  return fn(ctx) == 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
 
 // Host code cannot take the address of a __device__ array directly: its
-// device address comes from cudaGetSymbolAddress, once per device, with that
-// device current.
+// device address comes from cudaGetSymbolAddress, with the device current.
+// It is looked up on the first call on a device and again whenever the
+// current context is not the one it was looked up in (another context of the
+// same device, or the device's primary context created anew).
 cudaError_t noalloc_scratch(int dev, void **out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  ScratchSlot &slot = g_noalloc_slot[dev];
+  void *ctx = nullptr;
+  cudaError_t e = current_context(&ctx);
+  if (e != cudaSuccess) return e;
+  if (!slot.addr || !ctx || ctx != slot.ctx) {
     void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
+    e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);  // makes the device's context current if none was
     if (e != cudaSuccess) return e;
-    g_noalloc_addr[dev] = p;
+    e = current_context(&ctx);
+    if (e != cudaSuccess) return e;
+    slot.ctx = ctx;
+    slot.addr = p;
   }
-  *out = g_noalloc_addr[dev];
+  *out = slot.addr;
   return cudaSuccess;
 }
 
@@ -54,13 +86,18 @@ extern "C" pfdd_status pfdd_fft_device_noalloc(void *data, int n1, int n2, int n
     if (n[ax] < 1 || (n[ax] & (n[ax] - 1)) != 0) return PFDD_EINVAL;
     if (n[ax] > kNoAllocMaxLen) return PFDD_ELIMIT;  // beyond the static twiddle table
   }
+  const Geometry g = make_geometry(n1, n2, n3, 0, precision == PFDD_FP64 ? sizeof(double2) : sizeof(float2),
+                                   precision == PFDD_FP64 ? 8 : 4);
+  // grid sizes of the three passes: every launch covers all the data or none runs
+  if ((long long)batch * g.zNparts > INT_MAX || (long long)batch * n1 * g.tiles[0] > INT_MAX ||
+      (long long)batch * g.tiles[1] > INT_MAX)
+    return PFDD_EINVAL;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return PFDD_ECUDA;
   void *scratch = nullptr;
   if (noalloc_scratch(dev, &scratch) != cudaSuccess) return PFDD_ECUDA;
   cudaStream_t st = (cudaStream_t)stream;
   const int pc = precision == PFDD_FP64 ? 0 : 1;
-  const size_t vsize = pc == 0 ? sizeof(double2) : sizeof(float2);
   // every call rewrites the tables of its three lengths before using them
   void *tw[3];
   for (int ax = 0; ax < 3; ++ax) {
@@ -69,7 +106,6 @@ extern "C" pfdd_status pfdd_fft_device_noalloc(void *data, int n1, int n2, int n
     else twiddle_kernel<float><<<(n[ax] + 127) / 128, 128, 0, st>>>(tw[ax], n[ax]);
   }
   if (cudaGetLastError() != cudaSuccess) return PFDD_ECUDA;
-  const Geometry g = make_geometry(n1, n2, n3, 0, vsize, pc == 0 ? 8 : 4);
   ZParams zp;
   memset(&zp, 0, sizeof zp);
   zp.S = data; zp.tw = tw[2]; zp.N = (long long)n1 * n2 * n3; zp.lines_per_field = (long long)n1 * n2;

@@ -44,13 +44,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   return ok != 0;
 }
 
-// Waits for phase `parity` of the barrier for at most kWaitNs; false (and *err
-// set) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, int *err) {
+// Waits for phase `parity` of the barrier for at most limit_ns; false (and
+// *err set) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, int *err,
+                                          unsigned long long limit_ns = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > kWaitNs) {
+    if (global_ns() - t0 > limit_ns) {
       if (err) atomicOr(err, 1);
       return false;
     }

@@ -26,7 +26,13 @@ def native_lib():
 
 def golden_cases():
     """Trajectory cases (gamma per step and final xi of the reference's own run)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("strain_"))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("strain_", "oracle_")))
+
+
+def golden_steps(spec, z) -> int:
+    """Steps the reference ran for a golden case: the whole ramp, or the prefix
+    ``steps_run`` of it (the ramp divisor stays ``spec.steps``)."""
+    return int(z["steps_run"]) if "steps_run" in z else spec.steps
 
 
 def strain_golden_cases():

@@ -52,14 +52,14 @@ def spec_json(spec: workloads.SolveSpec) -> str:
     return json.dumps(d)
 
 
-def run_case(name: str, spec: workloads.SolveSpec, fp64: bool):
+def run_case(name: str, spec: workloads.SolveSpec, fp64: bool, krun: int | None = None):
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=fp64,
                               asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)
         refio.write_xi_files(d, xi, bc, ns_ref=12)
-        build_ref.run_ref(b, d)
+        build_ref.run_ref(b, d, krun=krun)
         g = refio.read_gamma_full(d / "gamma_full.dat")
         xf = refio.read_xi_file(d / "xi.dat", spec.n, 12 + refio.NV)
         return g, xf[:spec.ns]
@@ -72,16 +72,18 @@ def sample_points(npts: int, count: int, seed: int) -> np.ndarray:
     return np.sort(rng.choice(npts, size=min(count, npts), replace=False))
 
 
-def make(name: str, spec: workloads.SolveSpec):
+def make(name: str, spec: workloads.SolveSpec, krun: int | None = None):
+    """krun: the reference runs only the first ``krun`` steps of the spec's K-step
+    ramp (a prefix of the full solve; the ramp divisor stays K)."""
     with ThreadPoolExecutor(2) as ex:
-        f64 = ex.submit(run_case, name, spec, True)
-        f32 = ex.submit(run_case, name, spec, False)
+        f64 = ex.submit(run_case, name, spec, True, krun)
+        f32 = ex.submit(run_case, name, spec, False, krun)
         (g64, x64), (g32, x32) = f64.result(), f32.result()
-    K = spec.steps
+    K = spec.steps if krun is None else krun
     assert g64.shape[0] == K, f"{name}: reference stopped after {g64.shape[0]} steps"
     npts = spec.npts
     xi0, _ = workloads.initial_state(spec)
-    out = dict(spec=spec_json(spec), gamma=g64[:, 1], gamma_a=g64[:, 2:2 + spec.ns],
+    out = dict(spec=spec_json(spec), steps_run=np.array(K), gamma=g64[:, 1], gamma_a=g64[:, 2:2 + spec.ns],
                gamma_fp32ref=g32[:, 1], gamma_a_fp32ref=g32[:, 2:2 + spec.ns],
                xi0_checksum=np.array([xi0.real.sum(), (xi0.real ** 2).sum()]),
                xi_final_checksum=np.array([x64.real.sum(), x64.imag.sum(), (np.abs(x64) ** 2).sum()]),
@@ -95,6 +97,45 @@ def make(name: str, spec: workloads.SolveSpec):
         out["xi_final_sample"] = flat[:, idx]
     np.savez_compressed(OUT / f"{name}.npz", **out)
     print(f"{name}: K={K} gamma[-1]={g64[-1, 1]:.6e} fp32-ref max|dxi|={float(out['fp32ref_max_dxi']):.2e}")
+
+
+def prefix_cases():
+    """Prefixes of full-size solves: (name, spec, steps run).  The 128^3 x 12
+    config-1 solve (8 seeded loops, sigma_xz ramp 0 -> 0.05 over K = 1000
+    steps): its first 5 steps, so the reference's setup (Bmatrix at 128^3)
+    dominates the generation time."""
+    yield "config1_128c_ns12_prefix5", workloads.config1(), 5
+
+
+def make_oracle_long(name: str = "oracle_config1_128c_ns12_k1000", every: int = 100, keep=(100, 1000)):
+    """The whole 1000-step config-1 solve (128^3 x 12) run by the CPU FP64
+    restatement (oracle/pfdd_cpu.c), which the reference-generated cases pin to the
+    reference itself (at 128^3 through config1_128c_ns12_prefix5): gamma and gamma_a
+    of every step and a seeded sample of xi at the steps ``keep``.  The reference
+    at this size runs for hours on one core; the restatement on all cores in
+    minutes."""
+    import oracle as orc
+    spec = workloads.config1()
+    eps = orc.fcc_eps(spec.ns, dslip=np.full(12, spec.dslip))
+    C44, C12 = spec.mu, spec.lam
+    B = orc.bmatrix(spec.n, eps, 2.0 * C44 + C12, C12, C44, spec.d)
+    sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
+    tau = orc.ramp_tau(orc.resolved_shear(eps, sig), spec.steps)
+    xi, bc = workloads.initial_state(spec)
+    idx = sample_points(spec.npts, 1024, seed=4242)
+    gs, gas, samples = [], [], []
+    ns = spec.ns
+    for s0 in range(0, spec.steps, every):
+        xi, g, ga = orc.run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf),
+                            np.full(ns, spec.dslip), 1.0, tau[s0:s0 + every])
+        gs.append(g); gas.append(ga)
+        if s0 + every in keep:
+            samples.append(xi.reshape(ns, -1)[:, idx])
+        print(f"{name}: step {s0 + every} gamma={g[-1]:.9e}", flush=True)
+    out = dict(spec=spec_json(spec), gamma=np.concatenate(gs), gamma_a=np.concatenate(gas), sample_idx=idx,
+               sample_steps=np.array(keep), xi_samples=np.stack(samples),
+               generator=np.array("oracle/pfdd_cpu.c (FP64 restatement)"))
+    np.savez_compressed(OUT / f"{name}.npz", **out)
 
 
 def strain_cases():
@@ -145,6 +186,11 @@ if __name__ == "__main__":
     for nm, sp in cases():
         if not want or nm in want:
             make(nm, sp)
+    for nm, sp, kr in prefix_cases():
+        if not want or nm in want:
+            make(nm, sp, krun=kr)
+    if not want or "oracle_config1_128c_ns12_k1000" in want:
+        make_oracle_long()
     for nm, sp in strain_cases():
         if not want or nm in want:
             make_strain(nm, sp)

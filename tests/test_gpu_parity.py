@@ -7,7 +7,7 @@ FP64 oracle."""
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import GOLDEN, golden_cases, golden_steps, load_golden
 from oracle import oracle
 from pfdd_gb300 import native, workloads
 
@@ -38,8 +38,9 @@ def rel(a, b):
 @pytest.mark.parametrize("name", golden_cases())
 def test_fp64_matches_reference_golden(native_lib, name):
     spec, z = load_golden(name)
-    xf, g, ga, launches = run_gpu(spec)
-    assert launches >= spec.steps * 4
+    K = golden_steps(spec, z)
+    xf, g, ga, launches = run_gpu(spec, steps=K)
+    assert launches >= K * 4
     assert rel(g, z["gamma"]) <= GAMMA_RTOL
     assert np.max(np.abs(ga - z["gamma_a"])) <= GAMMA_RTOL * max(1e-3, np.max(np.abs(z["gamma_a"])))
     flat = xf.reshape(spec.ns, -1)

@@ -1,0 +1,104 @@
+"""Both forms at full size against the CPU FP64 oracle, and the whole 1000-step
+config-1 solve against the oracle's committed trajectory.
+
+The oracle (oracle/pfdd_cpu.c) matches the reference's own FP64 run to <= 1e-12
+on every golden case, including the first 5 steps of this very 128^3 x 12 solve
+(tests/golden/config1_128c_ns12_prefix5.npz, generated by the patched reference).
+
+Tolerances: plain FP64 form max|dxi| <= 1e-10 and gamma relative error <= 1e-9;
+FP32-FFT forms max|dxi| <= 1e-5 and gamma relative error <= 1e-5 (gamma of these
+runs stays away from zero)."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+from oracle import oracle
+from pfdd_gb300 import native, workloads
+
+pytestmark = pytest.mark.gpu
+
+XI_TOL = 1e-10
+GAMMA_RTOL = 1e-9
+FP32_TOL = 1e-5
+
+
+def run_gpu(spec, precision, steps, every=None):
+    """`steps` steps of `spec`'s ramp; with `every`, the state after each block of
+    `every` steps is returned too."""
+    s = native.solver_for(spec, precision)
+    try:
+        x0, b0 = workloads.initial_state(spec)
+        s.set_state(x0, b0)
+        tau = native.spec_tau(spec)[:steps]
+        gs, gas, states = [], [], {}
+        blk = every or steps
+        for s0 in range(0, steps, blk):
+            g, ga = s.step(tau[s0:s0 + blk])
+            gs.append(g[:, 0]); gas.append(ga[:, 0])
+            if every:
+                states[s0 + blk] = s.get_state()[0]
+        return s.get_state()[0], np.concatenate(gs), np.concatenate(gas), states
+    finally:
+        s.close()
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def rel_curve(a, b):
+    """Relative error of a curve that crosses zero (the config-1 gamma does near
+    step 300): |a - b| over max(|b|, 1e-3 max|b|), so the points next to the
+    crossing are held to 1e-3 of the curve's scale instead of to ~0."""
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3 * np.max(np.abs(b)))))
+
+
+def test_config1_128c_ns12_both_forms_full_field_vs_oracle(native_lib):
+    """The config-1 solve (128^3 x 12, 8 seeded loops, sigma_xz ramp over K = 1000),
+    its first 10 steps: every point of every field against the oracle."""
+    spec = workloads.config1()
+    K = 10
+    xo, go, gao = oracle.solve(spec, steps=K)
+    x64, g64, ga64, _ = run_gpu(spec, "fp64", K)
+    assert np.max(np.abs(x64 - xo)) <= XI_TOL
+    assert rel(g64, go) <= GAMMA_RTOL
+    assert np.max(np.abs(ga64 - gao)) <= GAMMA_RTOL * np.max(np.abs(gao))
+    for form in ("fp32", "fp32_bfly"):
+        x32, g32, _, _ = run_gpu(spec, form, K)
+        assert np.max(np.abs(x32 - xo)) <= FP32_TOL, form
+        assert rel(g32, go) <= FP32_TOL, form
+
+
+@pytest.mark.parametrize("ns", [3, 12])
+def test_256c_both_forms_full_field_vs_oracle(native_lib, ns):
+    """The largest grid of the serving mix (256^3), the longest z, y and x lines
+    the step compiles (LG = 8 on every axis), both slip-system counts of the mix."""
+    n = (256, 256, 256)
+    spec = workloads.SolveSpec(n=n, ns=ns, steps=200, sigma_max=0.05, noise_seed=256 + ns,
+                               loops=workloads.random_loops(n, 4, 4.0, 256 / 6, ns, seed=256 + ns))
+    K = 2
+    xo, go, gao = oracle.solve(spec, steps=K)
+    x64, g64, ga64, _ = run_gpu(spec, "fp64", K)
+    assert np.max(np.abs(x64 - xo)) <= XI_TOL
+    assert rel(g64, go) <= GAMMA_RTOL
+    x32, g32, _, _ = run_gpu(spec, "fp32", K)
+    assert np.max(np.abs(x32 - xo)) <= FP32_TOL
+    assert rel(g32, go) <= FP32_TOL
+
+
+def test_config1_1000_steps_vs_oracle_trajectory(native_lib):
+    """The whole config-1 solve: gamma and gamma_a of all 1000 steps and sampled
+    xi after 100 and 1000 steps, plain FP64 form, against the oracle's committed
+    trajectory (tests/golden/oracle_config1_128c_ns12_k1000.npz)."""
+    path = GOLDEN / "oracle_config1_128c_ns12_k1000.npz"
+    if not path.exists():
+        pytest.skip("trajectory fixture not generated")
+    spec, z = load_golden(path.stem)
+    idx = z["sample_idx"]
+    keep = [int(v) for v in z["sample_steps"]]
+    _, g, ga, states = run_gpu(spec, "fp64", spec.steps, every=100)
+    assert rel_curve(g, z["gamma"]) <= GAMMA_RTOL
+    assert np.max(np.abs(ga - z["gamma_a"])) <= GAMMA_RTOL * np.max(np.abs(z["gamma_a"]))
+    for q, st in enumerate(keep):
+        got = states[st].reshape(spec.ns, -1)[:, idx]
+        assert np.max(np.abs(got - z["xi_samples"][q])) <= XI_TOL, st

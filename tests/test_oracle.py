@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden, strain_golden_cases
+from conftest import golden_cases, golden_steps, load_golden, strain_golden_cases
 from oracle import oracle
 from pfdd_gb300 import workloads
 
@@ -13,7 +13,7 @@ def test_oracle_matches_patched_reference(name):
     xi0, _ = workloads.initial_state(spec)
     # the inputs regenerate bit-identically from the spec
     np.testing.assert_array_equal(z["xi0_checksum"], [xi0.real.sum(), (xi0.real ** 2).sum()])
-    xf, g, ga = oracle.solve(spec)
+    xf, g, ga = oracle.solve(spec, steps=golden_steps(spec, z))
     assert g.shape == z["gamma"].shape
     rel = np.max(np.abs(g - z["gamma"]) / np.maximum(np.abs(z["gamma"]), 1e-300))
     assert rel <= 1e-12, rel
