@@ -171,8 +171,21 @@ def b_table_bytes(prec: str, n, ns: int, plan: dict | None = None) -> float:
 
 
 def algorithmic_bytes(kernel: str, prec: str, n_pts: int, rf: int, ns: int, b_bytes: float = 0.0) -> float:
-    """Compulsory DRAM bytes of one launch (read + write once what the kernel
-    must touch); b_bytes: the stored B(k) the x-pass reads."""
+    """Algorithmic DRAM bytes of one launch: each kernel's share of the compulsory
+    bytes of a fully fused step, N*[ns*(16+16) + the B(k) table] (one read and one
+    write of the complex128 state, one read of the stored B(k)).  The z-pass owns
+    the state's read and write, the x-pass the B(k) read; the intermediate passes
+    over the spectral buffer are not algorithmic (they are in kernel_bytes)."""
+    if kernel in ("z_step", "plane"):
+        return rf * n_pts * 32.0             # FP64 xi in/out
+    if kernel in ("contract", "x_fused"):
+        return b_bytes
+    return 0.0
+
+
+def kernel_bytes(kernel: str, prec: str, n_pts: int, rf: int, ns: int, b_bytes: float = 0.0) -> float:
+    """Bytes one launch of this design's kernel must move when nothing comes from
+    L2: algorithmic_bytes plus its pass over the spectral buffer S."""
     v = 16 if prec == "fp64" else 8          # complex spectral element
     if kernel in ("z_step", "plane"):
         return rf * n_pts * (2 * v + 32)     # S in/out + FP64 xi in/out
@@ -413,28 +426,49 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
 
 def precision_curve(native, workloads, spec, dev, every=100, form="fp32"):
     """Config 2's report: the FP32-FFT form `form` against the plain FP64 form (which
-    matches the reference's FP64 run) on the same inputs over the whole
-    1000-step ramp, every `every` steps: max |dxi|, the largest |d gamma| so
-    far, that over the largest |gamma| so far (the curve crosses zero, where a
-    pointwise relative error means nothing), and the pointwise one."""
+    matches the reference's FP64 run and the oracle's 1000-step trajectory) on the
+    same inputs over the whole ramp, every `every` steps: max |dxi|; the relative
+    error of the average plastic strain at that step (the stated criterion) and the
+    largest within the block; and the largest |d gamma| so far over the largest
+    |gamma| so far (meaningful where gamma crosses zero, as config 1's does near
+    step 300, where the pointwise relative error has no scale)."""
     x0, b0 = workloads.initial_state(spec)
     tau = native.spec_tau(spec)
     ctx = {}
     for prec in (form, "fp64"):
         ctx[prec] = native.solver_for(spec, prec, device=dev)
         ctx[prec].set_state(x0, b0)
-    out, worst, dmax, gmax = [], 0.0, 0.0, 0.0
+    out, dmax, gmax = [], 0.0, 0.0
+    g32_all, g64_all = [], []
     for s0 in range(0, spec.steps, every):
         g = {p: c.step(tau[s0:s0 + every])[0][:, 0] for p, c in ctx.items()}
+        g32_all.append(g[form]); g64_all.append(g["fp64"])
         d = np.abs(g[form] - g["fp64"])
-        worst = max(worst, float(np.max(d / np.abs(g["fp64"]))))
+        pw = d / np.abs(g["fp64"])
         dmax, gmax = max(dmax, float(d.max())), max(gmax, float(np.abs(g["fp64"]).max()))
         dxi = float(np.max(np.abs(ctx[form].get_state() - ctx["fp64"].get_state())))
-        out.append({"step": s0 + every, "max_dxi": dxi, "max_dgamma": dmax, "dgamma_over_max_gamma": dmax / gmax,
-                    "gamma_pointwise_rel_err": worst, "gamma_fp64": float(g["fp64"][-1])})
+        out.append({"step": s0 + every, "max_dxi": dxi, "gamma_fp64": float(g["fp64"][-1]),
+                    "gamma_rel_err": float(pw[-1]), "gamma_rel_err_block_max": float(pw.max()),
+                    "max_dgamma": dmax, "dgamma_over_max_gamma": dmax / gmax})
     for c in ctx.values():
         c.close()
-    return out
+    g32, g64 = np.concatenate(g32_all), np.concatenate(g64_all)
+    pw = np.abs(g32 - g64) / np.abs(g64)
+    big = np.abs(g64) >= 0.01 * np.max(np.abs(g64))
+    tol = 1e-5
+    summary = {
+        "criterion": "relative error of the average plastic strain against the FP64 form <= 1e-5",
+        "pointwise_at_every_100_steps": max(e["gamma_rel_err"] for e in out),
+        "pointwise_all_steps": float(pw.max()),
+        "pointwise_where_abs_gamma_ge_1pct_of_max": float(pw[big].max()),
+        "steps_with_abs_gamma_below_1pct_of_max": int((~big).sum()),
+        "max_normalised_all_steps": out[-1]["dgamma_over_max_gamma"],
+        "meets": {"pointwise_at_every_100_steps": max(e["gamma_rel_err"] for e in out) <= tol,
+                  "pointwise_all_steps": bool(pw.max() <= tol),
+                  "pointwise_where_abs_gamma_ge_1pct_of_max": bool(pw[big].max() <= tol),
+                  "max_normalised_all_steps": out[-1]["dgamma_over_max_gamma"] <= tol},
+    }
+    return {"curve": out, "summary": summary}
 
 
 def time_strain(native, workloads, spec, dev, reps=3):
@@ -559,12 +593,17 @@ def run_ours(a):
             kern[nm] = {"launches": cnt, "avg_us": 1e3 * tot / cnt}
         cnt, tot = ks[top]
         avg_s = tot / cnt / 1e3
-        ab = algorithmic_bytes(top, head, spec.npts, spec.ns, spec.ns, b_table_bytes(head, spec.n, spec.ns, rh["plan"]))
+        bb = b_table_bytes(head, spec.n, spec.ns, rh["plan"])
+        ab = algorithmic_bytes(top, head, spec.npts, spec.ns, spec.ns, bb)
+        kb = kernel_bytes(top, head, spec.npts, spec.ns, spec.ns, bb)
         ach = ab / avg_s / 1e9
         tr = profiled_traffic(top, head, a.n, spec.ns)
         roof = {"bound": "hbm", "kernel": top, "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(ach / peaks["hbm_gbs"], 4), "traffic": tr, "algorithmic_bytes": ab,
-                "peak_src": peaks["src"] + " (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback"}
+                "kernel_bytes": kb, "kernel_bytes_gbs": round(kb / avg_s / 1e9, 1), "avg_us": round(avg_s * 1e6, 2),
+                "peak_src": peaks["src"] + " (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback",
+                "what": "achieved = the kernel's share of the step's algorithmic bytes (xi in/out for the z-pass) / "
+                        "its average launch time; kernel_bytes adds its pass over the spectral buffer"}
     # compulsory bytes of a step: xi in and out (and the B(k) table when stored)
     step_bytes = spec.npts * spec.ns * 32 + b_table_bytes(head, spec.n, spec.ns, rh["plan"])
     cpu = None

@@ -155,8 +155,9 @@ pfdd_status pfdd_kernel_stat(pfdd_ctx *ctx, int idx, const char **name, long lon
  * array, setstress F:3820-3918).  Outputs, each may be NULL: eps[9][N] and
  * sigma[9][N] (component 3*i + j, the real parts of DATAEPS and DATASIGMA),
  * aveps[9] and avesigma[9].  Needs the constants and eigenstrains of
- * pfdd_build_B.  Uses about (ns + 6)*N complex doubles of temporary device
- * memory for the call; the state is not changed. */
+ * pfdd_build_B.  Its work buffers, about (ns + 6)*N complex doubles plus 9*N
+ * doubles for each field output requested, are allocated by the first call and
+ * kept by the context until pfdd_destroy; the state is not changed. */
 pfdd_status pfdd_strain_stress(pfdd_ctx *ctx, int r, const double *sigma_app, double *eps, double *sigma,
                                double *aveps, double *avesigma);
 

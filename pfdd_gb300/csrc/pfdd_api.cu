@@ -26,6 +26,23 @@
 
 namespace pfdd {
 
+static std::mutex g_sm_mu;
+static int g_sm_count[kMaxDevices] = {};
+
+cudaError_t device_sm_count(int *out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaDeviceGetAttribute(out, cudaDevAttrMultiProcessorCount, dev);
+  std::lock_guard<std::mutex> lk(g_sm_mu);
+  if (!g_sm_count[dev]) {
+    e = cudaDeviceGetAttribute(&g_sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  *out = g_sm_count[dev];
+  return cudaSuccess;
+}
+
 __global__ void fill_u64_kernel(unsigned long long *p, long long n, unsigned long long v) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     p[i] = v;
@@ -407,6 +424,12 @@ struct pfdd_ctx {
   // allocation of pfdd_create fail (PFDD_ENOMEM)
   int drop_bulk = 0;
   int alloc_count = 0, fail_alloc_at = 0;
+  // work buffers of pfdd_strain_stress, allocated by its first call and kept
+  // (a free inside a running server would synchronise the whole device)
+  pfdd_fft_plan *sp_plan = nullptr;
+  double2 *sp_E = nullptr;
+  double *sp_eps = nullptr, *sp_sig = nullptr, *sp_part = nullptr;
+  StrainParams *sp_dp = nullptr;
 };
 
 // wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
@@ -682,7 +705,8 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
                 c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2],
-                c->xt, c->xtoff, c->xline, c->xord};
+                c->xt, c->xtoff, c->xline, c->xord, c->sp_E, c->sp_eps, c->sp_sig, c->sp_part, c->sp_dp};
+  if (c->sp_plan) pfdd_fft_plan_destroy(c->sp_plan);
   if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
   for (void *p : dp)
@@ -980,7 +1004,9 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   xp.err = c->errflag;
   xp.drop_bulk = c->drop_bulk;
   xp.wait_ns = c->drop_bulk ? kTestWaitNs : kWaitNs;
-  cudaError_t e = c->g.xWarp
+  cudaError_t e = c->g.xPipe
+                      ? launch_x_pipe_f32(c->ns, (long long)blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
+                  : c->g.xWarp
                       ? launch_x_warp_f32(c->ns, c->prec == PFDD_FFT_FP32_BFLY, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
                   : c->prec == PFDD_FFT_FP32_BFLY
                       ? launch_x_fused_f32_bfly(c->ns, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
@@ -1025,11 +1051,12 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   char b[1024];  // the fixed part; the autotune timings follow
   snprintf(b, sizeof b,
            "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld, \"warp_teams\": %d, "
+           "\"pipelined\": %d, "
            "\"b_tiles\": %lld, \"b_mirrored\": %d}, "
            "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
            "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
            "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": ",
-           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp,
+           1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp, (int)g.xPipe,
            g.xTable ? c->ntiles : 0LL, (int)(g.xTable && c->xtSym), 1 << g.lgTI[0], g.threads[0], g.smem[0],
            g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
            radix_plan(c->n[1], fft_nv(ilog2(c->n[1]))).c_str(), radix_plan(c->n[2], zpass_nv(ilog2(c->n[2]), vs)).c_str(),
@@ -1042,7 +1069,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
   int zTL, xLgT, yLgTI;
-  bool xWide, xWarp;
+  bool xWide, xWarp, xPipe;
   std::string timings;
 };
 static std::mutex g_plan_mu;
@@ -1062,9 +1089,10 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,x=<tile columns>,w=<0|1>,y=<tile columns>,f=<0|1>"
+  // PFDD_PLAN="z=<lines>,x=<tile columns>,w=<0|1|2>,y=<tile columns>,f=<0|1>"
   // pins the plan (each entry optional, ignored when it does not fit; w=1, the
-  // warp-team x-pass, after x; f=0, the y passes in ascending field order)
+  // warp-team x-pass, w=2 its persistent pipelined form, after x; f=0, the y
+  // passes in ascending field order)
   // instead of timing it, e.g. to profile the plan a timed run chose (a
   // profiler distorts the timings)
   if (const char *pin = std::getenv("PFDD_PLAN")) {
@@ -1081,7 +1109,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
                         : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v), false,
                                                       false, tt)
                         : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false,
-                                                      v == 1, tt)
+                                                      v >= 1, tt, v == 2)
                         : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs)
                                      : false;
         if (ok) c->g = g;
@@ -1104,7 +1132,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
         Geometry g = c->g;
         if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
             set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide,
-                           it->second.xWarp, uses_tile_table(c->prec) ? c->ntiles : 0) &&
+                           it->second.xWarp, uses_tile_table(c->prec) ? c->ntiles : 0, it->second.xPipe) &&
             (c->n[1] == 1 ||
              set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs))) {
           c->g = g;
@@ -1163,20 +1191,22 @@ static pfdd_status autotune(pfdd_ctx *c) {
     }
     c->g = best;
     bt = 1e30;
-    // tile widths 1..64, each with the block-team kernel (plain and wide) and
-    // the warp-team kernel (key suffix "v"); all compute the same bits
-    for (int cand = 0; cand <= 3 * 7 - 1; ++cand) {
-      const int lgT = cand / 3, form = cand % 3;
-      const bool wide = form == 1, warp = form == 2;
+    // tile widths 1..64, each with the block-team kernel (plain and wide), the
+    // warp-team kernel (key suffix "v") and its persistent pipelined form
+    // (suffix "p", tile table with line pairs); all compute the same bits
+    for (int cand = 0; cand <= 4 * 7 - 1; ++cand) {
+      const int lgT = cand / 4, form = cand % 4;
+      const bool wide = form == 1, warp = form >= 2, pipe = form == 3;
       Geometry g = c->g;
       if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide, warp,
-                          uses_tile_table(c->prec) ? c->ntiles : 0))
+                          uses_tile_table(c->prec) ? c->ntiles : 0, pipe))
         continue;
       c->g = g;
       const double us = time_us([&] { return launch_x_fused<T>(c); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
-      snprintf(b, sizeof b, "%s\"%d%s\": %.1f", xs.empty() ? "" : ", ", 1 << lgT, wide ? "w" : (warp ? "v" : ""), us);
+      snprintf(b, sizeof b, "%s\"%d%s\": %.1f", xs.empty() ? "" : ", ", 1 << lgT,
+               wide ? "w" : (pipe ? "p" : (warp ? "v" : "")), us);
       xs += b;
     }
     c->g = best;
@@ -1208,7 +1238,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
              ys + "}}";
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.xWide, c->g.xWarp, tuning};
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.xWide, c->g.xWarp, c->g.xPipe, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }
@@ -1535,22 +1565,30 @@ extern "C" pfdd_status pfdd_strain_stress(pfdd_ctx *c, int r, const double *sigm
         hp.sig[a][i][j] = s;
         hp.eps[a][i][j] = c->epsv[(a * 3 + i) * 3 + j];
       }
-  // FP64 work: a natural-layout FFT plan whose buffer holds the state's transform
-  pfdd_fft_plan *p = nullptr;
-  pfdd_status st = pfdd_fft_plan_create(&p, c->n[0], c->n[1], c->n[2], PFDD_FP64, std::max(ns, 6), c->dev);
-  if (st != PFDD_OK) return fail(c, st, "pfdd_strain_stress: work buffers (%s)", pfdd_status_string(st));
+  // FP64 work: a natural-layout FFT plan whose buffer holds the state's
+  // transform, the six strain components and the outputs; allocated by the
+  // first call, kept by the context
+  if (!c->sp_plan) {
+    pfdd_status st = pfdd_fft_plan_create(&c->sp_plan, c->n[0], c->n[1], c->n[2], PFDD_FP64, std::max(ns, 6), c->dev);
+    if (st != PFDD_OK) {
+      c->sp_plan = nullptr;
+      return fail(c, st, "pfdd_strain_stress: work buffers (%s)", pfdd_status_string(st));
+    }
+  }
+  pfdd_fft_plan *p = c->sp_plan;
   const int blocks = (int)std::min<long long>(1216, (N + 255) / 256);
-  double2 *E = nullptr;
-  double *d_eps = nullptr, *d_sig = nullptr, *part = nullptr;
-  StrainParams *dp = nullptr;
+  if (!c->sp_E) CK(c, cudaMalloc(&c->sp_E, 6 * N * sizeof(double2)));
+  if (eps && !c->sp_eps) CK(c, cudaMalloc(&c->sp_eps, 9 * N * sizeof(double)));
+  if (sigma && !c->sp_sig) CK(c, cudaMalloc(&c->sp_sig, 9 * N * sizeof(double)));
+  if (!c->sp_part) CK(c, cudaMalloc(&c->sp_part, 1216 * 18 * sizeof(double)));
+  if (!c->sp_dp) CK(c, cudaMalloc(&c->sp_dp, sizeof(StrainParams)));
+  double2 *E = c->sp_E;
+  double *d_eps = eps ? c->sp_eps : nullptr, *d_sig = sigma ? c->sp_sig : nullptr, *part = c->sp_part;
+  StrainParams *dp = c->sp_dp;
   std::vector<double2> dc(ns);
   std::vector<double> hpart((size_t)blocks * 18);
   double2 *W = reinterpret_cast<double2 *>(p->buf);
-  cudaError_t e = cudaMalloc(&E, 6 * N * sizeof(double2));
-  if (e == cudaSuccess && eps) e = cudaMalloc(&d_eps, 9 * N * sizeof(double));
-  if (e == cudaSuccess && sigma) e = cudaMalloc(&d_sig, 9 * N * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&part, hpart.size() * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof hp);
+  cudaError_t e = cudaSuccess;
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(W, c->xi + (size_t)r * ns * N, (size_t)ns * N * sizeof(double2), cudaMemcpyDeviceToDevice, p->st);
   if (e == cudaSuccess) e = fft_exec(p, W, ns, -1);
@@ -1607,9 +1645,6 @@ extern "C" pfdd_status pfdd_strain_stress(pfdd_ctx *c, int r, const double *sigm
       if (avesigma) avesigma[q] = ss / (double)N;
     }
   }
-  for (void *q : {(void *)E, (void *)d_eps, (void *)d_sig, (void *)part, (void *)dp})
-    if (q) cudaFree(q);
-  pfdd_fft_plan_destroy(p);
   CK(c, e);
   return PFDD_OK;
 }
