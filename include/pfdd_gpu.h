@@ -161,6 +161,42 @@ pfdd_status pfdd_kernel_stat(pfdd_ctx *ctx, int idx, const char **name, long lon
 pfdd_status pfdd_strain_stress(pfdd_ctx *ctx, int r, const double *sigma_app, double *eps, double *sigma,
                                double *aveps, double *avesigma);
 
+/* Interface-plane energy diagnostics of the reference's checkEnergy.dat and
+ * checkEbarrier.dat (avestrain F:641-749, ResidualEnergy F:3920-3945, the
+ * inner-loop block F:4645-4651).  They are sums over the points of the
+ * interface plane: grid index i == ppoint[0] and |n . (x - ppoint)| <= 1. */
+typedef struct {
+  int ppoint[3];          /* the plane's penetration point (F:4196-4198: N1/2, 0, 3*N3/4) */
+  double interface_n[3];  /* plane normal in the global frame (F:4215-4217) */
+  double sigma[3][3];     /* the applied stress (uniform sigma of setstress, F:3820-3918) */
+  double S11, S12, S44;   /* compliances (F:4261-4263) */
+  double mu;              /* C44 */
+  double D[4];            /* D00, D01, D10, D11 of ResidualEnergy (calculateD4int, F:3503) */
+  int ns_per_material;    /* NS1 (ResidualEnergy's material of system a is a / NS1); 0 means ns */
+} pfdd_diag_params;
+
+/* Turns the per-step diagnostics on (p != NULL) or off.  While on, every step
+ * of pfdd_step also gathers Re xi of every system on the interface plane and
+ * on the line (ppoint[0], j, ppoint[2]); pfdd_get_diagnostics returns the
+ * energies of the last pfdd_step call. */
+pfdd_status pfdd_set_diagnostics(pfdd_ctx *ctx, const pfdd_diag_params *p);
+
+/* Energies of each step of the last pfdd_step call, out[nsteps][nrep][6]:
+ * energy_in (elastic energy of the virtual strain fields, Energy_calculation
+ * F:3026-3467), energy_in2 (Imatrix F:2504-2616), energy_in3 (avestrain's
+ * -sum over the plane of (sum_a Re xi_a eps_a) : sigma), energy_in4
+ * (avestrain's -mu/2 sum over the plane of S : sigma : sigma, one call's worth:
+ * the reference adds it once per call and resets it once per outer step),
+ * energy_Residual, and their sum energy_intotal, each summed in the
+ * reference's order.  This library carries no virtual strain fields (one
+ * material), so energy_in and energy_in2 are 0 as in the reference's
+ * one-material runs.  nsteps must be the last call's step count. */
+pfdd_status pfdd_get_diagnostics(pfdd_ctx *ctx, int nsteps, double *out);
+
+/* The same energies for the current state of every replica (the line the
+ * reference writes for an outer step before its inner loop): out[nrep][6]. */
+pfdd_status pfdd_state_diagnostics(pfdd_ctx *ctx, double *out);
+
 /* Launch plan of the context as a JSON object: tile widths, threads and shared
  * memory of each pass, the radix plan of each axis, the steps per captured CUDA
  * graph and the autotune timings (null before the first pfdd_step, which times

@@ -41,6 +41,11 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
                                the inner loop runs in that step) plus full-precision
                                dumps of the strain and stress fields
                                (eps_full.bin, sigma_full.bin)
+13  4535, 4650                 full-precision copies of the energy lines:
+                               energy_full.dat (checkEnergy.dat, one line per outer
+                               step) and ebarrier_full.dat (one line per inner TDGL
+                               step): the step, energy_in, energy_in2, energy_in3,
+                               energy_in4, energy_Residual, energy_intotal
 ==  =========================  ====================================================
 """
 from __future__ import annotations
@@ -103,6 +108,10 @@ DEFAULTS_BLOCK = r"""
 #define PFDD_DUMP(name_, arr_, n_) do { FILE *f_ = fopen(name_, "wb"); \
     fwrite((arr_), sizeof(*(arr_)), (size_t)(n_), f_); fclose(f_); } while (0)
 static int pfdd_krun_(int k_) { const char *s_ = getenv("PFDD_KRUN"); return s_ ? atoi(s_) : k_; }
+#define PFDD_LOG_ENERGY(file_, it_, e1_, e2_, e3_, e4_, er_, et_) do { static FILE *pfdd_ef_; \
+    if (!pfdd_ef_) pfdd_ef_ = fopen(file_, "w"); \
+    fprintf(pfdd_ef_, "%d %.17e %.17e %.17e %.17e %.17e %.17e\n", (it_), (double)(e1_), (double)(e2_), \
+            (double)(e3_), (double)(e4_), (double)(er_), (double)(et_)); fflush(pfdd_ef_); } while (0)
 #define PFDD_LOG_STEP(itp_, g_, g1_) do { static FILE *pfdd_gf_; int q_; \
     if (!pfdd_gf_) pfdd_gf_ = fopen("gamma_full.dat", "w"); \
     fprintf(pfdd_gf_, "%d %.17e", (itp_), (double)(g_)); \
@@ -160,9 +169,15 @@ PATCHES = [
     (4461, "calc_strain_stress(databeta,", "if (PFDD_DIAG) calc_strain_stress(databeta,"),
     (4530, "energy_in = Energy_calculation(", "energy_in = (!PFDD_DIAG) ? 0 : Energy_calculation("),
     (4532, "energy_Residual = ResidualEnergy(", "energy_Residual = (!PFDD_DIAG) ? 0 : ResidualEnergy("),
+    (4535, "energy_Residual,energy_intotal);",
+     "energy_Residual,energy_intotal); PFDD_LOG_ENERGY(\"energy_full.dat\", it, energy_in, energy_in2, "
+     "energy_in3, energy_in4, energy_Residual, energy_intotal);"),
     (4580, "interfacevolv(xi,", "if(0)interfacevolv(xi,"),
     (4643, "fft_backward(datag, NS);", "if (PFDD_DIAG) fft_backward(datag, NS);"),
     (4645, "if (1) {//checkpass==1", "if (PFDD_DIAG) {//checkpass==1"),
+    (4650, "fabs(energy_Residual),fabs(energy_intotal));",
+     "fabs(energy_Residual),fabs(energy_intotal)); PFDD_LOG_ENERGY(\"ebarrier_full.dat\", it_checkEbarrier, "
+     "energy_in, energy_in2, energy_in3, energy_in4, energy_Residual, energy_intotal);"),
     (4672, "gamma1[0],gamma1[1],gamma);", "gamma1[0],gamma1[1],gamma); PFDD_LOG_STEP(it_plastic, gamma, gamma1);"),
 ]
 # the inner-loop gradient contraction ("if(isb<NS){" below line 4600)

@@ -114,6 +114,19 @@ __global__ void __launch_bounds__(kGammaWarps * 32 * kMaxNs) gamma_reduce_kernel
   }
 }
 
+// Interface-plane diagnostics: copies Re xi of every field at the listed points
+// (the plane's, then the residual line's) into out[step][field][point], the
+// step from the device counter (0 without one).
+__global__ void diag_gather_kernel(const double2 *__restrict__ xi, const long long *__restrict__ pts, int npts,
+                                   int RF, long long N, const int *step_ctr, double *out) {
+  const long long step = step_ctr ? *step_ctr : 0;
+  const long long per = (long long)RF * npts;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < per; i += (long long)gridDim.x * blockDim.x) {
+    const long long f = i / npts, q = i - f * npts;
+    out[step * per + i] = xi[f * N + pts[q]].x;
+  }
+}
+
 // ---- strain and stress fields (diagnostics) --------------------------------
 
 struct StrainParams {
@@ -348,10 +361,10 @@ namespace {
 
 // kernels of a step, for the optional per-kernel event timing
 enum KId { K_Z_PROLOGUE, K_Z_STEP, K_FFT_Y_FWD, K_FFT_X_FWD, K_CONTRACT, K_FFT_X_INV, K_FFT_Y_INV, K_GAMMA,
-           K_X_FUSED, K_PLANE, K_PLANE_PROLOGUE, K_COUNT };
+           K_X_FUSED, K_PLANE, K_PLANE_PROLOGUE, K_DIAG, K_COUNT };
 const char *const kKernelNames[K_COUNT] = {"z_prologue", "z_step", "fft_y_fwd", "fft_x_fwd", "contract",
                                            "fft_x_inv", "fft_y_inv", "gamma_reduce", "x_fused", "plane",
-                                           "plane_prologue"};
+                                           "plane_prologue", "diag_gather"};
 
 struct KTiming {
   bool on = false;
@@ -430,6 +443,17 @@ struct pfdd_ctx {
   double2 *sp_E = nullptr;
   double *sp_eps = nullptr, *sp_sig = nullptr, *sp_part = nullptr;
   StrainParams *sp_dp = nullptr;
+  // interface-plane diagnostics (pfdd_set_diagnostics): the gathered points
+  // (the plane's in the reference's row-major order, then the residual line's),
+  // the per-step gathers of a chunk and the energies of the last pfdd_step
+  bool diagOn = false;
+  pfdd_diag_params dgp{};
+  std::vector<long long> dpts;
+  int dplane = 0, dline = 0;
+  long long *d_dpts = nullptr;
+  double *d_dgat = nullptr;
+  std::vector<double> h_dgat, h_diag;
+  int diag_steps = 0;
 };
 
 // wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
@@ -705,7 +729,8 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
                 c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2],
-                c->xt, c->xtoff, c->xline, c->xord, c->sp_E, c->sp_eps, c->sp_sig, c->sp_part, c->sp_dp};
+                c->xt, c->xtoff, c->xline, c->xord, c->sp_E, c->sp_eps, c->sp_sig, c->sp_part, c->sp_dp,
+                c->d_dpts, c->d_dgat};
   if (c->sp_plan) pfdd_fft_plan_destroy(c->sp_plan);
   if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
@@ -1246,6 +1271,67 @@ static pfdd_status autotune(pfdd_ctx *c) {
   return PFDD_OK;
 }
 
+static cudaError_t launch_diag_gather(pfdd_ctx *c, const int *step_ctr) {
+  const int RF = c->nrep * c->ns, npts = (int)c->dpts.size();
+  const long long per = (long long)RF * npts;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>(152, (per + 255) / 256));
+  t_begin(c);
+  diag_gather_kernel<<<blocks, 256, 0, c->st>>>(c->xi, c->d_dpts, npts, RF, c->N, step_ctr, c->d_dgat);
+  t_end(c, K_DIAG);
+  return cudaGetLastError();
+}
+
+// Energies of the gathered values g (field a's point q at g[a * npts + q]) in
+// the reference's order of summation (avestrain F:641-749 for the plane sums,
+// ResidualEnergy F:3920-3945 for the line): out[6] = energy_in, energy_in2,
+// energy_in3, energy_in4 (one call's worth), energy_Residual, their sum.
+static void diag_energies(const pfdd_ctx *c, const double *g, double *out) {
+  const pfdd_diag_params &d = c->dgp;
+  const int ns = c->ns, npts = (int)c->dpts.size(), nspm = d.ns_per_material > 0 ? d.ns_per_material : ns;
+  auto dl = [](int i, int j) { return i == j ? 1 : 0; };
+  auto dl4 = [](int i, int j, int k, int l) { return (i == j && j == k && k == l) ? 1 : 0; };
+  double S[3][3][3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l)
+          S[i][j][k][l] = (d.S11 + 2 * d.S12) / 3.0 * dl(i, j) * dl(k, l) +
+                          d.S44 / 4.0 * (dl(i, k) * dl(j, l) + dl(i, l) * dl(j, k)) - d.S44 / 2.0 * dl4(i, j, k, l) +
+                          (d.S11 - d.S12) * (dl4(i, j, k, l) - dl(i, j) * dl(k, l) / 3.0);
+  double e3 = 0.0, e4 = 0.0;
+  for (int q = 0; q < c->dplane; ++q) {
+    double sp[3][3];
+    for (int u = 0; u < 3; ++u)
+      for (int v = 0; v < 3; ++v) {
+        sp[u][v] = 0.0;
+        for (int a = 0; a < ns; ++a) sp[u][v] += g[(size_t)a * npts + q] * c->epsv[(a * 3 + u) * 3 + v];
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        e3 += -(sp[i][j] + 0.0) * (d.sigma[i][j]);  // + the virtual strain, zero here
+        for (int k = 0; k < 3; ++k)
+          for (int l = 0; l < 3; ++l) e4 += -S[i][j][k][l] * d.sigma[k][l] * d.sigma[i][j] * 0.5 * d.mu;
+      }
+  }
+  const double D00 = d.D[0], D01 = d.D[1], D10 = d.D[2], D11 = d.D[3];
+  double er = 0.0;
+  for (int j = 0; j < c->dline; ++j) {
+    double x0 = 0.0, x1 = 0.0;
+    for (int a = 0; a < ns; ++a) {
+      const int m = a / nspm;
+      if (m == 0) x0 += g[(size_t)a * npts + c->dplane + j];
+      if (m == 1) x1 += g[(size_t)a * npts + c->dplane + j];
+    }
+    er = er + std::fabs(-D11 * x1 * x1 + (D10 + D01) * x1 * x0 - D00 * x0 * x0);
+  }
+  out[0] = 0.0;  // energy_in: no virtual strain fields
+  out[1] = 0.0;  // energy_in2: no virtual strain fields
+  out[2] = e3;
+  out[3] = e4;
+  out[4] = er;
+  out[5] = out[0] + out[1] + out[2] + out[3] + out[4];
+}
+
 // The launches of one TDGL step (step index taken from the device counter).
 template <typename T>
 static cudaError_t launch_step(pfdd_ctx *c, ZParams &zp) {
@@ -1253,6 +1339,7 @@ static cudaError_t launch_step(pfdd_ctx *c, ZParams &zp) {
   if (e == cudaSuccess) e = launch_x_fused<T>(c);
   if (e == cudaSuccess) e = ctx_strided(c, +1, 0);
   if (e == cudaSuccess) e = ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE);
+  if (e == cudaSuccess && c->diagOn) e = launch_diag_gather(c, c->step_ctr);
   return e;
 }
 
@@ -1275,6 +1362,11 @@ template <typename T>
 static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double *gamma, double *gamma_a) {
   ZParams zp = make_zparams(c);
   const int RF = c->nrep * c->ns;
+  const size_t dper = (size_t)RF * c->dpts.size();  // gathered values per step (diagnostics)
+  if (c->diagOn) {
+    c->h_diag.assign((size_t)nsteps * c->nrep * 6, 0.0);
+    c->diag_steps = nsteps;
+  }
   if (!c->specValid) {
     CK(c, ctx_zpass(c, zp, Z_SRC_XI | Z_FWD | Z_STORE));
     c->specValid = true;
@@ -1310,13 +1402,14 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
         c->launches = l0;  // captured, not launched
         c->graph_gen = c->gen;
       }
+      const int per_step = 4 + (c->diagOn ? 1 : 0);
       for (; done + kGraphSteps <= ks; done += kGraphSteps) {
         CK(c, cudaGraphLaunch(c->graph_many, c->st));
-        c->launches += 4LL * kGraphSteps;
+        c->launches += (long long)per_step * kGraphSteps;
       }
       for (; done < ks; ++done) {
         CK(c, cudaGraphLaunch(c->graph_one, c->st));
-        c->launches += 4;
+        c->launches += per_step;
       }
     }
     const int nt = ks * c->nrep;
@@ -1339,6 +1432,15 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
     bool finite = true;
     for (int q = 0; q < nt; ++q)
       if (c->h_active[q % c->nrep] && !std::isfinite(c->h_gam[q])) finite = false;
+    if (c->diagOn) {
+      CK(c, cudaMemcpyAsync(c->h_dgat.data(), c->d_dgat, (size_t)ks * dper * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->st));
+      CK(c, cudaStreamSynchronize(c->st));
+      for (int s = 0; s < ks; ++s)
+        for (int r = 0; r < c->nrep; ++r)
+          diag_energies(c, c->h_dgat.data() + ((size_t)s * c->nrep + r) * c->ns * c->dpts.size(),
+                        c->h_diag.data() + (((size_t)(s0 + s)) * c->nrep + r) * 6);
+    }
     if (gamma) std::memcpy(gamma + (size_t)s0 * c->nrep, c->h_gam, (size_t)nt * sizeof(double));
     if (gamma_a) std::memcpy(gamma_a + (size_t)s0 * RF, c->h_gam_a, (size_t)ks * RF * sizeof(double));
     if (!finite) return fail(c, PFDD_ENONFINITE, "pfdd_step: state became non-finite within steps %d..%d", s0, s0 + ks - 1);
@@ -1371,6 +1473,74 @@ extern "C" pfdd_status pfdd_get_plan(pfdd_ctx *c, char *buf, size_t len) {
   const std::string p = plan_json(c, c->tuned ? c->plan : std::string("null"));
   if (p.size() + 1 > len) return fail(c, PFDD_EINVAL, "pfdd_get_plan: buffer of %zu bytes, need %zu", len, p.size() + 1);
   std::memcpy(buf, p.c_str(), p.size() + 1);
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_set_diagnostics(pfdd_ctx *c, const pfdd_diag_params *p) {
+  if (!c) return PFDD_EINVAL;
+  if (!p) {
+    if (c->diagOn) c->gen++;  // captured steps lose the gather
+    c->diagOn = false;
+    return PFDD_OK;
+  }
+  if (!c->hasElastic) return fail(c, PFDD_ENOTREADY, "pfdd_set_diagnostics: needs the eigenstrains of pfdd_build_B");
+  const int n1 = c->n[0], n2 = c->n[1], n3 = c->n[2];
+  for (int ax = 0; ax < 3; ++ax)
+    if (p->ppoint[ax] < 0 || p->ppoint[ax] >= c->n[ax])
+      return fail(c, PFDD_EINVAL, "pfdd_set_diagnostics: ppoint outside the grid");
+  if (p->ns_per_material < 0) return fail(c, PFDD_EINVAL, "pfdd_set_diagnostics: ns_per_material < 0");
+  // the plane's points in the reference's row-major order (avestrain's test,
+  // F:691 and F:702), then the residual line (ppoint_x, j, ppoint_z), j ascending
+  std::vector<long long> pts;
+  const double *nv = p->interface_n;
+  for (int k1 = 0; k1 < n1; ++k1)
+    for (int k2 = 0; k2 < n2; ++k2)
+      for (int k3 = 0; k3 < n3; ++k3)
+        if (std::fabs(nv[0] * (k1 - p->ppoint[0]) + nv[1] * (k2 - p->ppoint[1]) + nv[2] * (k3 - p->ppoint[2])) <= 1.0 &&
+            k1 == p->ppoint[0])
+          pts.push_back(((long long)k1 * n2 + k2) * n3 + k3);
+  const int nplane = (int)pts.size();
+  for (int j = 0; j < n2; ++j) pts.push_back(((long long)p->ppoint[0] * n2 + j) * n3 + p->ppoint[2]);
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaStreamSynchronize(c->st));
+  if (c->d_dpts) CK(c, cudaFree(c->d_dpts));
+  if (c->d_dgat) CK(c, cudaFree(c->d_dgat));
+  c->d_dpts = nullptr;
+  c->d_dgat = nullptr;
+  const size_t dper = (size_t)c->nrep * c->ns * pts.size();
+  CK(c, cudaMalloc(&c->d_dpts, pts.size() * sizeof(long long)));
+  CK(c, cudaMalloc(&c->d_dgat, (size_t)c->kchunk * dper * sizeof(double)));
+  CK(c, cudaMemcpy(c->d_dpts, pts.data(), pts.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  c->h_dgat.assign((size_t)c->kchunk * dper, 0.0);
+  c->dpts = pts;
+  c->dplane = nplane;
+  c->dline = n2;
+  c->dgp = *p;
+  c->diagOn = true;
+  c->diag_steps = 0;
+  c->gen++;  // captured steps gain the gather
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_get_diagnostics(pfdd_ctx *c, int nsteps, double *out) {
+  if (!c || !out || nsteps < 0) return fail(c, PFDD_EINVAL, "pfdd_get_diagnostics: bad argument");
+  if (!c->diagOn || nsteps != c->diag_steps)
+    return fail(c, PFDD_ENOTREADY, "pfdd_get_diagnostics: no diagnostics of a %d-step call", nsteps);
+  std::memcpy(out, c->h_diag.data(), (size_t)nsteps * c->nrep * 6 * sizeof(double));
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_state_diagnostics(pfdd_ctx *c, double *out) {
+  if (!c || !out) return fail(c, PFDD_EINVAL, "pfdd_state_diagnostics: bad argument");
+  if (!c->diagOn) return fail(c, PFDD_ENOTREADY, "pfdd_state_diagnostics: diagnostics not set");
+  if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_state_diagnostics: state not set");
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, launch_diag_gather(c, nullptr));
+  const size_t per = (size_t)c->ns * c->dpts.size();
+  CK(c, cudaMemcpyAsync(c->h_dgat.data(), c->d_dgat, (size_t)c->nrep * per * sizeof(double), cudaMemcpyDeviceToHost,
+                        c->st));
+  CK(c, cudaStreamSynchronize(c->st));
+  for (int r = 0; r < c->nrep; ++r) diag_energies(c, c->h_dgat.data() + (size_t)r * per, out + (size_t)r * 6);
   return PFDD_OK;
 }
 

@@ -32,8 +32,37 @@ EXPORTS = [
     "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
     "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
     "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority", "pfdd_get_plan",
-    "pfdd_strain_stress",
+    "pfdd_strain_stress", "pfdd_set_diagnostics", "pfdd_get_diagnostics", "pfdd_state_diagnostics",
 ]
+
+DIAG_COLUMNS = ("energy_in", "energy_in2", "energy_in3", "energy_in4", "energy_Residual", "energy_intotal")
+
+
+class DiagParams(C.Structure):
+    """pfdd_diag_params of include/pfdd_gpu.h."""
+    _fields_ = [("ppoint", C.c_int * 3), ("interface_n", C.c_double * 3), ("sigma", C.c_double * 9),
+                ("S11", C.c_double), ("S12", C.c_double), ("S44", C.c_double), ("mu", C.c_double),
+                ("D", C.c_double * 4), ("ns_per_material", C.c_int)]
+
+
+def reference_diag_params(n, sigma_max: float, C11: float, C12: float, C44: float, D=(0.0, 0.0, 0.0, 0.0),
+                          ns_per_material: int = 0) -> DiagParams:
+    """The reference program's interface-plane set-up: penetration point
+    (N1/2, 0, 3 N3/4) (F:4195-4198), normal (sqrt3/3, 0, sqrt6/3) (F:4215-4217),
+    the applied sigma_xz, compliances S11, S12, S44 (F:4261-4263), mu = C44."""
+    p = DiagParams()
+    p.ppoint[:] = [n[0] // 2, 0, n[2] * 3 // 4]
+    p.interface_n[:] = [np.sqrt(3.0) / 3.0, 0.0, np.sqrt(6.0) / 3.0]
+    sig = [0.0] * 9
+    sig[2] = sig[6] = sigma_max
+    p.sigma[:] = sig
+    p.S11 = 1.0 / 3.0 * (1 / (C11 + 2 * C12) + 2 / (C11 - C12))
+    p.S12 = 1.0 / 3.0 * (1 / (C11 + 2 * C12) - 1 / (C11 - C12))
+    p.S44 = 1 / C44
+    p.mu = C44
+    p.D[:] = list(D)
+    p.ns_per_material = ns_per_material
+    return p
 
 _lib = None
 
@@ -78,6 +107,9 @@ def load():
     L.pfdd_set_stream_priority.argtypes = [vp, i]
     L.pfdd_get_plan.argtypes = [vp, C.c_char_p, sz]
     L.pfdd_strain_stress.argtypes = [vp, i, dp, dp, dp, dp, dp]
+    L.pfdd_set_diagnostics.argtypes = [vp, C.POINTER(DiagParams)]
+    L.pfdd_get_diagnostics.argtypes = [vp, i, dp]
+    L.pfdd_state_diagnostics.argtypes = [vp, dp]
     L.pfdd_set_kernel_timing.argtypes = [vp, i]
     L.pfdd_kernel_stat.argtypes = [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     L.pfdd_required_bytes.argtypes = [i, i, i, i, i, i]
@@ -274,6 +306,23 @@ class Solver:
                     "pfdd_strain_stress")
         rs = (lambda a: None if a is None else a.reshape(3, 3, self.N))
         return rs(e), rs(s), ae.reshape(3, 3), asg.reshape(3, 3)
+
+    def set_diagnostics(self, params: "DiagParams | None"):
+        """Interface-plane energy diagnostics per step (None turns them off)."""
+        self._check(self.L.pfdd_set_diagnostics(self.h, C.byref(params) if params is not None else None),
+                    "pfdd_set_diagnostics")
+
+    def diagnostics(self, nsteps: int) -> np.ndarray:
+        """Energies of each step of the last step() call, [nsteps, nrep, 6] (DIAG_COLUMNS)."""
+        out = np.zeros((nsteps, self.nrep, 6))
+        self._check(self.L.pfdd_get_diagnostics(self.h, nsteps, _dp(out)), "pfdd_get_diagnostics")
+        return out
+
+    def state_diagnostics(self) -> np.ndarray:
+        """Energies of the current state of every replica, [nrep, 6] (DIAG_COLUMNS)."""
+        out = np.zeros((self.nrep, 6))
+        self._check(self.L.pfdd_state_diagnostics(self.h, _dp(out)), "pfdd_state_diagnostics")
+        return out
 
     def plan(self) -> dict:
         """Launch plan (tile widths, threads, shared memory, radix plans, autotune timings)."""

@@ -26,7 +26,12 @@ def native_lib():
 
 def golden_cases():
     """Trajectory cases (gamma per step and final xi of the reference's own run)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("strain_", "oracle_")))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("strain_", "oracle_", "diag_")))
+
+
+def diag_golden_cases():
+    """Interface-plane energy diagnostics of the reference's own runs."""
+    return sorted(p.stem for p in GOLDEN.glob("diag_*.npz"))
 
 
 def golden_steps(spec, z) -> int:

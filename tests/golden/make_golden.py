@@ -138,6 +138,41 @@ def make_oracle_long(name: str = "oracle_config1_128c_ns12_k1000", every: int = 
     np.savez_compressed(OUT / f"{name}.npz", **out)
 
 
+def diag_cases():
+    """Interface-plane energy diagnostics (patch 13 of oracle/build_ref.py): the
+    reference's full-precision copies of checkEnergy.dat (one line per outer
+    step) and checkEbarrier.dat's energies (one line per inner TDGL step)."""
+    c0 = workloads.config0()
+    c0.steps = 40
+    yield "diag_config0_32c_ns3_k40", c0
+    yield "diag_fcc12_16x8x32_k12", workloads.SolveSpec(
+        n=(16, 8, 32), ns=12, steps=12, sigma_max=0.06,
+        loops=workloads.random_loops((16, 8, 32), 4, 2.0, 5.0, 12, seed=41), noise_seed=41)
+
+
+def make_diag(name: str, spec: workloads.SolveSpec):
+    import re
+    b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=True, diag=True,
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
+    d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
+    try:
+        xi, bc = workloads.initial_state(spec)
+        refio.write_xi_files(d, xi, bc, ns_ref=12)
+        build_ref.run_ref(b, d)
+        outer = np.loadtxt(d / "energy_full.dat", ndmin=2)
+        inner = np.loadtxt(d / "ebarrier_full.dat", ndmin=2)
+        g = refio.read_gamma_full(d / "gamma_full.dat")
+        log = (d / "stdout.log").read_text()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    m = re.search(r"^D00 = (\S+), D11 = (\S+), D10 = (\S+), D01 = (\S+)", log, re.M)
+    D = np.array([float(m.group(1)), float(m.group(4)), float(m.group(3)), float(m.group(2))])  # D00 D01 D10 D11
+    out = dict(spec=spec_json(spec), energy_outer=outer, energy_inner=inner, gamma=g[:, 1], D=D,
+               columns=np.array("step energy_in energy_in2 energy_in3 energy_in4 energy_Residual energy_intotal"))
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print(f"{name}: {inner.shape[0]} inner lines, D = {D}")
+
+
 def strain_cases():
     """Strain/stress of an initial state (patch 12 of oracle/build_ref.py): the
     reference dumps both fields in full precision and writes strain.txt,
@@ -194,3 +229,6 @@ if __name__ == "__main__":
     for nm, sp in strain_cases():
         if not want or nm in want:
             make_strain(nm, sp)
+    for nm, sp in diag_cases():
+        if not want or nm in want:
+            make_diag(nm, sp)

@@ -102,3 +102,22 @@ def test_config1_1000_steps_vs_oracle_trajectory(native_lib):
     for q, st in enumerate(keep):
         got = states[st].reshape(spec.ns, -1)[:, idx]
         assert np.max(np.abs(got - z["xi_samples"][q])) <= XI_TOL, st
+
+
+@pytest.mark.parametrize("form", ["fp32", "fp32_bfly"])
+def test_config2_precision_form_vs_oracle_trajectory(native_lib, form):
+    """Config 2: the FP32-FFT form on the config-1 problem over its 1000 steps
+    against the FP64 oracle's trajectory.  The criterion -- relative error of
+    the average plastic strain <= 1e-5, reported every 100 steps -- is checked
+    at steps 100, 200, ..., 1000.  gamma crosses zero at step 285 (|gamma| =
+    1e-6 there against 7e-3 at the end), where a pointwise relative error has
+    no scale, so over every step the error is held to 1e-5 of max|gamma|."""
+    path = GOLDEN / "oracle_config1_128c_ns12_k1000.npz"
+    if not path.exists():
+        pytest.skip("trajectory fixture not generated")
+    spec, z = load_golden(path.stem)
+    _, g, _, _ = run_gpu(spec, form, spec.steps)
+    gz = z["gamma"]
+    every = np.abs(g[99::100] - gz[99::100]) / np.abs(gz[99::100])
+    assert np.max(every) <= FP32_TOL, every
+    assert np.max(np.abs(g - gz)) <= FP32_TOL * np.max(np.abs(gz))
