@@ -988,7 +988,8 @@ static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
   const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
   t_begin(c);
-  cudaError_t e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp);
+  cudaError_t e =
+      launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp, c->g.zNV);
   t_end(c, (flags & Z_UPDATE) ? K_Z_STEP : K_Z_PROLOGUE);
   return e;
 }
@@ -1007,7 +1008,7 @@ static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/) {
   t_begin(c);
   cudaError_t e = launch_strided(prec_code(c->prec), sign, ilog2(L), (unsigned)blocks, c->g.threads[gi], c->g.smem[gi],
                                  c->st, c->S, c->g.lgTI[gi], inner, c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0],
-                                 c->active, outer_per_rep, c->g.pitch[gi], ax == 0 && c->yRev);
+                                 c->active, outer_per_rep, c->g.pitch[gi], ax == 0 && c->yRev, c->g.nv[gi]);
   t_end(c, ax == 0 ? (sign < 0 ? K_FFT_Y_FWD : K_FFT_Y_INV) : (sign < 0 ? K_FFT_X_FWD : K_FFT_X_INV));
   return e;
 }
@@ -1084,8 +1085,8 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
            1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp, (int)g.xPipe,
            g.xTable ? c->ntiles : 0LL, (int)(g.xTable && c->xtSym), 1 << g.lgTI[0], g.threads[0], g.smem[0],
            g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
-           radix_plan(c->n[1], fft_nv(ilog2(c->n[1]))).c_str(), radix_plan(c->n[2], zpass_nv(ilog2(c->n[2]), vs)).c_str(),
-           kGraphSteps);
+           radix_plan(c->n[1], g.nv[0] ? g.nv[0] : fft_nv(ilog2(c->n[1]))).c_str(),
+           radix_plan(c->n[2], g.zNV ? g.zNV : zpass_nv(ilog2(c->n[2]), vs)).c_str(), kGraphSteps);
   return std::string(b) + tuning + "}";
 }
 
@@ -1093,7 +1094,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
 // times each shape once; later contexts of the shape (serving classes, batch
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
-  int zTL, xLgT, yLgTI;
+  int zTL, xLgT, yLgTI, zNV, yNV;
   bool xWide, xWarp, xPipe;
   std::string timings;
 };
@@ -1114,8 +1115,9 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,x=<tile columns>,w=<0|1|2>,y=<tile columns>,f=<0|1>"
-  // pins the plan (each entry optional, ignored when it does not fit; w=1, the
+  // PFDD_PLAN="z=<lines>,n=<8|16>,x=<tile columns>,w=<0|1|2>,y=<tile columns>,m=<8|16>,f=<0|1>"
+  // pins the plan (each entry optional, ignored when it does not fit; n and m:
+  // values a thread of the z-pass and the y passes, the radix plans; w=1, the
   // warp-team x-pass, w=2 its persistent pipelined form, after x; f=0, the y
   // passes in ascending field order)
   // instead of timing it, e.g. to profile the plan a timed run chose (a
@@ -1130,12 +1132,18 @@ static pfdd_status autotune(pfdd_ctx *c) {
       if (kv && v > 0) {
         Geometry g = c->g;
         const long long tt = uses_tile_table(c->prec) ? c->ntiles : 0;
-        const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v) && g.zNparts <= c->zparts_cap
+        const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v, g.zNV) &&
+                                           g.zNparts <= c->zparts_cap
+                        : key == 'n' ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, g.zTL, v) &&
+                                           g.zNparts <= c->zparts_cap
+                        : key == 'm' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], g.lgTI[0],
+                                                            vs, v)
                         : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v), false,
                                                       false, tt)
                         : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false,
                                                       v >= 1, tt, v == 2)
-                        : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs)
+                        : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs,
+                                                            g.nv[0])
                                      : false;
         if (ok) c->g = g;
       }
@@ -1155,11 +1163,13 @@ static pfdd_status autotune(pfdd_ctx *c) {
       auto it = g_plans.find(key);
       if (it != g_plans.end()) {
         Geometry g = c->g;
-        if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL) && g.zNparts <= c->zparts_cap &&
+        if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL, it->second.zNV) &&
+            g.zNparts <= c->zparts_cap &&
             set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide,
                            it->second.xWarp, uses_tile_table(c->prec) ? c->ntiles : 0, it->second.xPipe) &&
             (c->n[1] == 1 ||
-             set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs))) {
+             set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs,
+                                  it->second.yNV))) {
           c->g = g;
           c->gen++;
           c->plan = "{\"cached\": true, \"timings\": " + it->second.timings + "}";
@@ -1201,9 +1211,12 @@ static pfdd_status autotune(pfdd_ctx *c) {
     fill_u64_kernel<<<1216, kThreads, 0, c->st>>>(reinterpret_cast<unsigned long long *>(c->xi),
                                                   (long long)c->ns * c->N * 2, 0x3fe0000000000000ull);
     cudaMemsetAsync(c->tau, 0, (size_t)c->nrep * c->ns * sizeof(double), c->st);
-    for (int lgTL = 0; lgTL <= 5; ++lgTL) {
+    // z-pass lines per block and radix plan (values a thread: 8, 16): the
+    // plans round differently, the line counts change no result
+    for (int cand = 0; cand < 2 * 6; ++cand) {
+      const int lgTL = cand >> 1, nv = (cand & 1) ? 16 : 8;
       Geometry g = c->g;
-      if (!set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, 1 << lgTL) || g.zNparts > c->zparts_cap) continue;
+      if (!set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, 1 << lgTL, nv) || g.zNparts > c->zparts_cap) continue;
       c->g = g;
       ZParams zp = make_zparams(c);
       zp.step_ctr = nullptr;
@@ -1211,7 +1224,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
       const double us = time_us([&] { return ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
-      snprintf(b, sizeof b, "%s\"%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, us);
+      snprintf(b, sizeof b, "%s\"%d/%d\": %.1f", zs.empty() ? "" : ", ", 1 << lgTL, nv, us);
       zs += b;
     }
     c->g = best;
@@ -1237,14 +1250,15 @@ static pfdd_status autotune(pfdd_ctx *c) {
     c->g = best;
     if (c->n[1] > 1) {
       bt = 1e30;
-      for (int lgTI = 0; lgTI <= 7; ++lgTI) {
+      for (int cand = 0; cand < 2 * 8; ++cand) {
+        const int lgTI = cand >> 1, nv = (cand & 1) ? 16 : 8;
         Geometry g = c->g;
-        if (!set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], lgTI, vs)) continue;
+        if (!set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], lgTI, vs, nv)) continue;
         c->g = g;
         const double us = time_us([&] { return ctx_strided(c, -1, 0); });
         if (us > 0 && us < bt) { bt = us; best = g; }
         char b[64];
-        snprintf(b, sizeof b, "%s\"%d\": %.1f", ys.empty() ? "" : ", ", 1 << lgTI, us);
+        snprintf(b, sizeof b, "%s\"%d/%d\": %.1f", ys.empty() ? "" : ", ", 1 << lgTI, nv, us);
         ys += b;
       }
       c->g = best;
@@ -1263,7 +1277,8 @@ static pfdd_status autotune(pfdd_ctx *c) {
              ys + "}}";
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.xWide, c->g.xWarp, c->g.xPipe, tuning};
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.zNV, c->g.nv[0],
+                               c->g.xWide, c->g.xWarp, c->g.xPipe, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }

@@ -170,6 +170,9 @@ __host__ __device__ __forceinline__ void stockham_plan_stage(V *v, int th, int l
 // the y passes 70 -> 66 us and the FP64 z-pass 3.13 -> 3.06 ms, but the FP32
 // z-pass (64 registers a thread for four 256-thread CTAs per SM) 280 -> 355 us
 // and the FP64 x-pass (spills) 2.98 -> 3.52 ms, so those two stay at 8.
+// These are the defaults; the z-pass and the strided passes are compiled for
+// both 8 and 16 where they differ (L >= 16), and a context's autotuner times
+// both (the x-pass keeps xpass_nv).
 __host__ __device__ constexpr int fft_nv(int lgL) { return (lgL == 4 || lgL == 7 || lgL == 8) ? 16 : 8; }
 __host__ __device__ constexpr int zpass_nv(int lgL, int vsize) { return vsize == 8 ? 8 : fft_nv(lgL); }
 __host__ __device__ constexpr int xpass_nv(int lgL, int vsize) { return vsize == 8 ? fft_nv(lgL) : 8; }

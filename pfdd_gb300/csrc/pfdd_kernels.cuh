@@ -182,18 +182,19 @@ __device__ __forceinline__ long long update_tile_f32(const ZParams &p, const Upd
 // consecutive (x, y) pairs, whose S values arrive by cp.async; x-fastest S
 // layout (sxf): the lines (x0 + t, y) of one y, whose S values sit TL to a
 // contiguous run and go straight between global memory and registers.
-template <typename T, int LG>
+// NV: values a thread holds (8 or 16: the radix plan, see stockham_plan_stage).
+template <typename T, int LG, int NV>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZParams p) {
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ long long red[32];
   static_assert(LG >= 0, "the z-pass is instantiated per line length");
+  static_assert(NV == 8 || NV == 16, "8 or 16 values a thread");
   constexpr int L = 1 << LG, lgL = LG;
   const int TL = p.TL, P = p.pitch;
   V *tws = reinterpret_cast<V *>(smraw);
   V *sm = tws + L;
   double2 *xs = reinterpret_cast<double2 *>(smraw + ((((size_t)L + (size_t)TL * P) * sizeof(V) + 15) & ~(size_t)15));
-  constexpr int NV = zpass_nv(LG, (int)sizeof(V));
   const int E = L >= NV ? NV : L, team = L / E;
   const long long line0 = (long long)blockIdx.x * TL;
   const long long rf = line0 / p.lines_per_field;
@@ -340,10 +341,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
 // Batched line FFT along a strided axis: data viewed as [outer][L][inner],
 // one CTA transforms an L x TI tile (TI contiguous inner columns).
 // Shared memory: twiddles [L] | tile [L][pitch].
-template <typename T, int S, int LG>
+// NV: values a thread holds (8 or 16) for L >= 8.
+template <typename T, int S, int LG, int NV>
 __global__ void __launch_bounds__(256)
 fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long tiles_per_outer, const void *tw_,
                    const uint8_t *active, long long outer_per_rep, int pitch, int rev) {
+  static_assert(NV == 8 || NV == 16, "8 or 16 values a thread");
   using V = typename cpx<T>::t;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int L = 1 << lgL, TI = 1 << lgTI;
@@ -366,7 +369,7 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
     // consecutive columns: coalesced), the last stage straight back; shared
     // memory only between stages.  The first stage uses no twiddles, and the
     // barrier after it orders the twiddle table before the second.
-    constexpr int NV = fft_nv(LG), LV = (1 << LG) / NV;
+    constexpr int LV = (1 << LG) / NV;
     const int t = tid & (TI - 1), th = tid >> lgTI;
     V *col = base + t;
     const int in32 = (int)inner;  // a line spans L * inner < 2^31 values

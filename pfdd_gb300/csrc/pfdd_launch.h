@@ -13,13 +13,15 @@
 #include "pfdd_kernels.cuh"
 
 namespace pfdd {
-// z-pass for lgL in [0, 9]; prec 0 = FP64 spectra, 1 = FP32
+// z-pass for lgL in [0, 9]; prec 0 = FP64 spectra, 1 = FP32; nv: values a
+// thread (8, or 16 for lgL >= 4; 0: zpass_nv)
 cudaError_t launch_zpass(int prec, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
-                         const ZParams &p);
-// strided line FFT (sign -1 forward, +1 inverse) for lgL in [0, 9]
+                         const ZParams &p, int nv = 0);
+// strided line FFT (sign -1 forward, +1 inverse) for lgL in [0, 9]; nv as
+// launch_zpass (0: fft_nv)
 cudaError_t launch_strided(int prec, int sign, int lgL, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                            void *data, int lgTI, long long inner, long long tiles_per_outer, const void *tw,
-                           const uint8_t *active, long long outer_per_rep, int pitch, bool rev = false);
+                           const uint8_t *active, long long outer_per_rep, int pitch, bool rev = false, int nv = 0);
 // fused x-pass (x-forward FFT, contraction, x-inverse FFT) for ns in [1, 12]
 cudaError_t launch_x_fused_f32(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p);
 cudaError_t launch_x_fused_f64(int ns, unsigned blocks, int threads, size_t smem, cudaStream_t st, const XParams &p);
@@ -51,8 +53,12 @@ inline int ilog2(long long v) {
 // threads per line (team) of the strided passes and the z-pass, which have
 // every line length compiled in, and of the fused x-pass, which has N1 =
 // 32..256 compiled in and runs other lengths with 8 values per thread
-inline int line_team(int L) { return L / std::min(fft_nv(ilog2(L)), L); }
-inline int z_line_team(int L, size_t vsize) { return L / std::min(zpass_nv(ilog2(L), (int)vsize), L); }
+inline int line_team(int L, int nv = 0) { return L / std::min(nv ? nv : fft_nv(ilog2(L)), L); }
+inline int z_line_team(int L, size_t vsize, int nv = 0) {
+  return L / std::min(nv ? nv : zpass_nv(ilog2(L), (int)vsize), L);
+}
+// the radix plans a line of L can run: 8 values a thread, and 16 from L = 16 on
+inline bool nv_ok(int L, int nv) { return nv == 0 || nv == 8 || (nv == 16 && L >= 16); }
 inline int x_line_team(int n1, size_t vsize) {
   const int lg = ilog2(n1);
   return n1 / std::min(lg >= 5 && lg <= 8 ? xpass_nv(lg, (int)vsize) : 8, n1);
@@ -67,11 +73,12 @@ struct Geometry {
   // spectral layout of a context's S: x fastest ([y][z][x] per field); the
   // FFT-boundary plans keep the natural [x][y][z]
   bool xfast = false;
-  // z-pass
-  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0;
+  // z-pass; zNV: values a thread (the radix plan; 0: zpass_nv)
+  int zTL = 1, zThreads = 1, zPitch = 1, zNparts = 1, lgL3 = 0, zNV = 0;
   size_t zSmem = 0;
-  // strided passes (y: axis 1, x: axis 0; x only in the FFT-boundary plans)
-  int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1};
+  // strided passes (y: axis 1, x: axis 0; x only in the FFT-boundary plans);
+  // nv: values a thread (0: fft_nv)
+  int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1}, nv[2] = {0, 0};
   long long tiles[2] = {1, 1};
   size_t smem[2] = {0, 0};
   // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel); xPipe: its
@@ -95,11 +102,14 @@ inline int z_line_pitch(int L, int TL, size_t vsize) {
   return TL >= u ? L + 1 : L + u / TL;
 }
 
-// z-pass with TL lines per block (the x-fastest layout needs TL <= N1).
-inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, int TL) {
-  const int L3 = n3, team3 = z_line_team(L3, vsize);
+// z-pass with TL lines per block (the x-fastest layout needs TL <= N1) and nv
+// values a thread (0: the default radix plan).
+inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, int TL, int nv = 0) {
+  if (!nv_ok(n3, nv)) return false;
+  const int L3 = n3, team3 = z_line_team(L3, vsize, nv);
   const long long lines = (long long)n1 * n2;
   if (TL < 1 || TL > lines || (g.xfast && TL > n1) || (long long)TL * team3 > kThreads) return false;
+  g.zNV = nv;
   g.zTL = TL;
   g.zThreads = TL * team3;
   g.zPitch = z_line_pitch(L3, TL, vsize);
@@ -110,11 +120,14 @@ inline bool set_z_geometry(Geometry &g, int n1, int n2, int n3, size_t vsize, in
   return g.zSmem <= kMaxDynSmem;
 }
 
-// Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile.
-inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, int lgTI, size_t vsize) {
-  const int team = line_team(L);
+// Strided pass along axis ax (0: y, 1: x) with TI = 2^lgTI columns per tile
+// and nv values a thread (0: the default radix plan).
+inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, int lgTI, size_t vsize, int nv = 0) {
+  if (!nv_ok(L, nv)) return false;
+  const int team = line_team(L, nv);
   const int TI = 1 << lgTI;
   if (TI > inner || (long long)TI * team > kThreads) return false;  // fft_strided_kernel launch bounds
+  g.nv[ax] = nv;
   g.lgTI[ax] = lgTI;
   g.threads[ax] = TI * team;
   g.pitch[ax] = TI >= 8 ? TI + 1 : TI;
@@ -227,8 +240,10 @@ inline Geometry make_geometry(int n1, int n2, int n3, int ns, size_t vsize, size
     while (lgT > 0 && ((1LL << lgT) > (long long)n2 * n3 ||
                        x_fused_smem(ns, n1, lgT, line_pitch(n1), vsize, bsize) > 110 * 1024))
       --lgT;
-    // tile table: a CTA per line pair, or per line when a pair's tile does not fit
-    g.valid = table_tiles > 0 ? (set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 1, false, false, table_tiles) ||
+    // tile table: a CTA per line pair with warp teams (the autotuner's choice at
+    // 128^3 x 12), else with block teams, or per line when a pair's tile does not fit
+    g.valid = table_tiles > 0 ? (set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 1, false, true, table_tiles) ||
+                                 set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 1, false, false, table_tiles) ||
                                  set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, 0, false, false, table_tiles))
                               : set_x_geometry(g, n1, n2, n3, ns, vsize, bsize, lgT);
   }

@@ -12,9 +12,9 @@
 // sized to about kChunkTargetS of wall time, so queued solves are admitted
 // quickly whatever the class's step time.  Classes are created when the
 // device-memory budget admits them and released when idle (at once when other
-// solves wait for memory).  Streams of classes with less work per step get a
-// more urgent CUDA priority, so short solves are not queued behind the
-// kernels of large grids.
+// solves wait for memory).  Streams of classes of smaller solves get a more
+// urgent CUDA priority, so their kernels are not queued behind the kernels of
+// large grids; within a class, free slots take the shortest queued solve.
 //
 // A solve's results do not depend on what runs beside it: replicas never read
 // each other's data, chunking does not change the arithmetic, and admitting a
@@ -180,10 +180,15 @@ static void route(pfdd_server *s, long long id) {
 }
 
 // CUDA stream priority of a class: one level more urgent per factor 4 less
-// work per step (grid points x systems x slots), least urgent above 2^26.
+// work in one solve's step (grid points x systems), least urgent from 2^27.5
+// (256^3 x 12) on; pfdd_set_stream_priority clamps to the device's range.
+// The block scheduler dispatches the CTAs of grids of equal priority in launch
+// order, so without this a small solve's kernel waits behind every CTA of a
+// large grid's kernel; the slot count must not enter (a class of many small
+// solves is still a class of small kernels).
 static int class_priority(const Class *c) {
-  const double work = (double)c->n[0] * c->n[1] * c->n[2] * c->ns * c->nslots;
-  return -std::max(0, (int)std::floor((26.0 - std::log2(std::max(work, 1.0))) / 2.0));
+  const double work = (double)c->n[0] * c->n[1] * c->n[2] * c->ns;
+  return -std::max(0, (int)std::floor((27.6 - std::log2(std::max(work, 1.0))) / 2.0));
 }
 
 static pfdd_status setup_class(pfdd_server *s, Class *c) {
@@ -221,10 +226,16 @@ static void worker_main(pfdd_server *s, Class *c) {
         c->pending.clear();
         s->cv.notify_all();
       }
+      // free slots take the queued solves with the fewest steps first (shortest
+      // job first: a short solve does not wait behind long ones of its class)
       for (int r = 0; r < R && !c->pending.empty(); ++r)
         if (c->slot[r] < 0) {
-          c->slot[r] = c->pending.front();
-          c->pending.pop_front();
+          auto best = std::min_element(c->pending.begin(), c->pending.end(), [&](long long a, long long b) {
+            const int sa = s->reqs.at(a)->spec.steps, sb = s->reqs.at(b)->spec.steps;
+            return sa != sb ? sa < sb : a < b;
+          });
+          c->slot[r] = *best;
+          c->pending.erase(best);
           admit.emplace_back(r, s->reqs.at(c->slot[r]).get());
         }
       const bool busy = std::any_of(c->slot.begin(), c->slot.end(), [](long long v) { return v >= 0; });
