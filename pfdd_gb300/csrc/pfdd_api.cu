@@ -1111,6 +1111,19 @@ static std::string plan_key(const pfdd_ctx *c) {
 // fastest.  Tile widths change no result: every line and every point is
 // computed by the same instructions whatever the tile.  The trial launches
 // overwrite the spectral buffer, which the next step rebuilds from xi.
+// A pinned radix plan with the widest tile (z lines per block, y columns) up
+// to the current one that fits its thread count.
+static bool pin_z_radix(const pfdd_ctx *c, Geometry &g, size_t vs, int nv) {
+  for (int TL = g.zTL; TL >= 1; TL >>= 1)
+    if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, TL, nv) && g.zNparts <= c->zparts_cap) return true;
+  return false;
+}
+static bool pin_y_radix(const pfdd_ctx *c, Geometry &g, size_t vs, int nv) {
+  for (int lgTI = g.lgTI[0]; lgTI >= 0; --lgTI)
+    if (set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], lgTI, vs, nv)) return true;
+  return false;
+}
+
 template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
@@ -1134,10 +1147,8 @@ static pfdd_status autotune(pfdd_ctx *c) {
         const long long tt = uses_tile_table(c->prec) ? c->ntiles : 0;
         const bool ok = key == 'z'   ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, v, g.zNV) &&
                                            g.zNparts <= c->zparts_cap
-                        : key == 'n' ? set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, g.zTL, v) &&
-                                           g.zNparts <= c->zparts_cap
-                        : key == 'm' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], g.lgTI[0],
-                                                            vs, v)
+                        : key == 'n' ? pin_z_radix(c, g, vs, v)
+                        : key == 'm' ? pin_y_radix(c, g, vs, v)
                         : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v), false,
                                                       false, tt)
                         : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false,

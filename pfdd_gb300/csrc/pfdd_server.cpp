@@ -73,6 +73,7 @@ struct Class {
   std::vector<long long> slot;  // request id per slot, -1 = free
   std::deque<long long> pending;
   size_t bytes = 0;
+  int priority = 0;  // CUDA stream priority (lower = more urgent), see class_priority
   std::thread worker;
 };
 
@@ -99,8 +100,36 @@ std::string class_key(const pfdd_request &r) {
 
 }  // namespace
 
+// Exclusive mode: one class's chunk of steps on the GPU at a time, the
+// waiting class of the most urgent priority first (ties in arrival order).
+struct TurnGate {
+  std::mutex mu;
+  std::condition_variable cv;
+  bool busy = false;
+  long long next_ticket = 0;
+  std::map<std::pair<int, long long>, int> waiting;  // (priority, ticket)
+
+  void acquire(int prio) {
+    std::unique_lock<std::mutex> lk(mu);
+    const auto key = std::make_pair(prio, next_ticket++);
+    waiting.emplace(key, 0);
+    cv.wait(lk, [&] { return !busy && waiting.begin()->first == key; });
+    waiting.erase(waiting.begin());
+    busy = true;
+  }
+  void release() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      busy = false;
+    }
+    cv.notify_all();
+  }
+};
+
 struct pfdd_server {
   int prec = 0, dev = 0, max_slots = 1, chunk = 1;
+  bool exclusive = false;
+  TurnGate gate;
   size_t budget = 0, reserved = 0, peak = 0;
   std::mutex mu;
   std::condition_variable cv;
@@ -194,7 +223,8 @@ static int class_priority(const Class *c) {
 static pfdd_status setup_class(pfdd_server *s, Class *c) {
   const int ns = c->ns;
   pfdd_status st = pfdd_create_batched(&c->ctx, c->n[0], c->n[1], c->n[2], ns, c->nslots, s->prec, s->dev);
-  if (st == PFDD_OK) st = pfdd_set_stream_priority(c->ctx, class_priority(c));
+  c->priority = class_priority(c);
+  if (st == PFDD_OK) st = pfdd_set_stream_priority(c->ctx, c->priority);
   if (st == PFDD_OK) st = pfdd_build_B(c->ctx, c->C[0], c->C[1], c->C[2], c->eps.data(), c->d[0], c->d[1], c->d[2]);
   if (st == PFDD_OK) {
     std::vector<double> v(ns, c->cd2), a(ns, c->asf), d(ns, c->dslip);
@@ -289,9 +319,11 @@ static void worker_main(pfdd_server *s, Class *c) {
                 act[r]->tau_max[a] * ((act[r]->progress + k + 1.0) / act[r]->spec.steps);
     g.assign((size_t)chunk * R, 0.0);
     ga.assign((size_t)chunk * R * ns, 0.0);
+    if (s->exclusive) s->gate.acquire(c->priority);
     const auto tc = Clock::now();
     const pfdd_status e = pfdd_step(c->ctx, chunk, tau.data(), g.data(), ga.data());
     const double dt = std::chrono::duration<double>(Clock::now() - tc).count();
+    if (s->exclusive) s->gate.release();
     step_s = step_s > 0 ? 0.5 * step_s + 0.5 * dt / chunk : dt / chunk;
     std::vector<int> finished;
     {
@@ -346,6 +378,7 @@ extern "C" pfdd_status pfdd_server_create(pfdd_server **out, int precision, int 
   s->prec = precision; s->dev = device; s->max_slots = max_slots; s->chunk = chunk_steps;
   s->budget = hbm_budget ? std::min(hbm_budget, freeb) : (size_t)(0.9 * (double)freeb);
   if (const char *p = std::getenv("PFDD_SERVER_TRACE")) s->trace_path = p;
+  if (const char *p = std::getenv("PFDD_SERVER_EXCLUSIVE")) s->exclusive = p[0] && p[0] != '0';
   *out = s;
   return PFDD_OK;
 }

@@ -45,7 +45,11 @@ def test_bounded_wait_timeout_is_reported_and_context_recovers(native_lib, monke
         xs = s.get_state()[0]
     finally:
         s.close()
+    if plan:  # the same launch plan (an autotuned one may pick another radix plan: other rounding)
+        monkeypatch.setenv("PFDD_PLAN", plan)
     r = native.solver_for(spec, form)
+    if plan:
+        monkeypatch.delenv("PFDD_PLAN")
     try:
         r.set_state(x0, b0)
         gr, _ = r.step(tau)
