@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--batched-steps", type=int, default=100,
                     help="timed steps of the 16-replica batched leg (0 skips it)")
     ap.add_argument("--batched-only", action="store_true", help="run only the batched leg, print its JSON")
-    ap.add_argument("--serve-scale", type=float, default=0.1,
-                    help="step-count scale of the 96-request serving mix (0 skips the serving leg)")
+    ap.add_argument("--serve-scale", type=float, default=1.0,
+                    help="step-count scale of the 96-request serving mix (1: the mix as specified, "
+                         "200-2000 steps a request; 0 skips the serving leg)")
     return ap.parse_args()
 
 

@@ -380,6 +380,9 @@ struct KTiming {
 struct pfdd_ctx {
   int n[3] = {0, 0, 0};
   int ns = 0, nrep = 0, prec = 0, dev = 0;
+  // replicas a step's grids cover: up to the last active one (idle replicas
+  // below it are skipped by the kernels; those above it cost no CTAs at all)
+  int krep = 0;
   long long N = 0;
   cudaStream_t st = nullptr;
   void *S = nullptr;
@@ -650,7 +653,7 @@ extern "C" pfdd_status pfdd_create_batched(pfdd_ctx **out, int n1, int n2, int n
   pfdd_ctx *c = new pfdd_ctx();
   *out = c;
   c->n[0] = n1; c->n[1] = n2; c->n[2] = n3;
-  c->ns = ns; c->nrep = nrep; c->prec = precision; c->dev = device;
+  c->ns = ns; c->nrep = nrep; c->krep = nrep; c->prec = precision; c->dev = device;
   c->N = (long long)n1 * n2 * n3;
   if (const char *v = std::getenv("PFDD_TEST_FAIL_ALLOC")) c->fail_alloc_at = std::atoi(v);
   CK(c, cudaSetDevice(device));
@@ -973,9 +976,26 @@ extern "C" pfdd_status pfdd_set_tau_field(pfdd_ctx *c, const double *tf) {
   return PFDD_OK;
 }
 
+// Grid extent of a step: replicas up to the last active one (at least one,
+// so an all-idle step still launches valid, empty grids).
+static void update_krep(pfdd_ctx *c) {
+  int k = 0;
+  for (int r = 0; r < c->nrep; ++r)
+    if (c->h_active[r]) k = r + 1;
+  k = std::max(k, 1);
+  if (k != c->krep) {
+    c->krep = k;
+    c->gen++;  // captured grid sizes change
+  }
+}
+
 extern "C" pfdd_status pfdd_set_replica_active(pfdd_ctx *c, int r, int on) {
   if (!c || r < 0 || r >= c->nrep) return fail(c, PFDD_EINVAL, "pfdd_set_replica_active: bad replica");
+  // a replica that was idle when the spectral buffer was last rebuilt from xi
+  // has no spectral state: the next step rebuilds it
+  if (on && !c->h_active[r]) c->specValid = false;
   c->h_active[r] = on ? 1 : 0;
+  update_krep(c);
   CK(c, cudaSetDevice(c->dev));
   CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), c->nrep, cudaMemcpyHostToDevice, c->st));
   CK(c, cudaStreamSynchronize(c->st));
@@ -986,7 +1006,7 @@ static int prec_code(int prec) { return prec == PFDD_FP64 ? 0 : 1; }
 
 static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
-  const long long blocks = (long long)c->nrep * c->ns * c->g.zNparts;
+  const long long blocks = (long long)c->krep * c->ns * c->g.zNparts;
   t_begin(c);
   cudaError_t e =
       launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp, c->g.zNV);
@@ -1001,9 +1021,9 @@ static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/) {
   // y lines: stride N3*N1 in the x-fastest layout, N3 in the natural one
   const long long inner = ax == 0 ? (c->g.xfast ? (long long)c->n[2] * c->n[0] : (long long)c->n[2])
                                   : (long long)c->n[1] * c->n[2];
-  const long long outer = ax == 0 ? (long long)c->nrep * c->ns * (c->g.xfast ? 1 : c->n[0])
-                                  : (long long)c->nrep * c->ns;
-  const long long outer_per_rep = outer / c->nrep;
+  const long long outer = ax == 0 ? (long long)c->krep * c->ns * (c->g.xfast ? 1 : c->n[0])
+                                  : (long long)c->krep * c->ns;
+  const long long outer_per_rep = outer / c->krep;
   const long long blocks = outer * c->g.tiles[gi];
   t_begin(c);
   cudaError_t e = launch_strided(prec_code(c->prec), sign, ilog2(L), (unsigned)blocks, c->g.threads[gi], c->g.smem[gi],
@@ -1022,9 +1042,9 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   xp.xline = c->g.xTable ? c->xline : nullptr;
   xp.xord = c->g.xTable ? c->xord : nullptr;
   xp.inner = (long long)c->n[1] * c->n[2]; xp.tiles = c->g.xTiles;
-  xp.L = c->n[0]; xp.lgL = ilog2(c->n[0]); xp.lgT = c->g.xLgT; xp.pitch = c->g.xPitch; xp.R = c->nrep;
+  xp.L = c->n[0]; xp.lgL = ilog2(c->n[0]); xp.lgT = c->g.xLgT; xp.pitch = c->g.xPitch; xp.R = c->krep;
   xp.step_ctr = c->step_ctr;
-  const unsigned blocks = (unsigned)(c->nrep * c->g.xTiles);
+  const unsigned blocks = (unsigned)(c->krep * c->g.xTiles);
   t_begin(c);
   xp.bf = c->bf;
   xp.err = c->errflag;
@@ -1210,11 +1230,13 @@ static pfdd_status autotune(pfdd_ctx *c) {
     double bt = 1e30;
     // the timings take one replica (the kernels skip idle ones), so tuning a
     // batched context costs what tuning one solve does
+    const int krep_saved = c->krep;
     if (c->nrep > 1) {
       std::vector<uint8_t> one(c->nrep, 0);
       one[0] = 1;
       CK(c, cudaMemcpyAsync(c->active, one.data(), c->nrep, cudaMemcpyHostToDevice, c->st));
       CK(c, cudaStreamSynchronize(c->st));
+      c->krep = 1;  // grids over replica 0 alone
     }
     // z-pass lines per block (the gamma partials are exact integer sums, so
     // the split of points into blocks changes no result); a typical state
@@ -1281,6 +1303,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
     if (c->nrep > 1) {  // every replica active again
       CK(c, cudaMemcpyAsync(c->active, c->h_active.data(), c->nrep, cudaMemcpyHostToDevice, c->st));
       CK(c, cudaStreamSynchronize(c->st));
+      c->krep = krep_saved;
     }
     c->specValid = false;
     c->gen++;  // captured launch shapes change

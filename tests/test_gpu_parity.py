@@ -341,3 +341,45 @@ def test_small_and_odd_system_counts_match_oracle(native_lib, ns):
         x32, g32, _, _ = run_gpu(spec, form, bc=bc)
         assert np.max(np.abs(x32 - xo)) <= 1e-5
         assert rel(g32, go) <= FP32_GAMMA_RTOL
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_trailing_idle_replicas_are_skipped(native_lib, prec):
+    """A step's grids cover the replicas up to the last active one: with the
+    last two of four idle, the active two equal their own runs bit for bit and
+    the idle ones keep their state; activating the last one widens the grids
+    again (the graphs are recaptured) with the same per-replica results."""
+    base = workloads.SolveSpec(n=(16, 16, 32), ns=3, steps=8, sigma_max=0.05,
+                               loops=[workloads.Loop(0, (8, 8, 16), 4.0)])
+    specs = [workloads.SolveSpec(**{**base.__dict__, "noise_seed": 70 + r}) for r in range(4)]
+    xs = np.stack([workloads.initial_state(sp)[0] for sp in specs])
+    bcs = np.stack([workloads.initial_state(sp)[1] for sp in specs])
+    tau = np.stack([native.spec_tau(sp) for sp in specs], axis=1)
+    s = native.solver_for(specs[0], prec, nrep=4)
+    try:
+        s.set_state(xs, bcs)
+        s.set_active(2, False)
+        s.set_active(3, False)
+        g1, _ = s.step(tau[:4])
+        x1 = s.get_state()
+        s.set_active(3, True)
+        g2, _ = s.step(tau[4:])
+        x2 = s.get_state()
+    finally:
+        s.close()
+    np.testing.assert_array_equal(x1[2], xs[2])
+    np.testing.assert_array_equal(x1[3], xs[3])
+    np.testing.assert_array_equal(x2[2], xs[2])
+    for r in (0, 1):
+        xr, gr, _, _ = run_gpu(specs[r], prec)
+        np.testing.assert_array_equal(x2[r], xr)
+        np.testing.assert_array_equal(np.concatenate([g1[:, r], g2[:, r]]), gr)
+    # replica 3 ran the last 4 steps of its ramp from its initial state
+    s3 = native.solver_for(specs[3], prec)
+    try:
+        s3.set_state(xs[3], bcs[3])
+        g3, _ = s3.step(native.spec_tau(specs[3])[4:])
+        np.testing.assert_array_equal(x2[3], s3.get_state()[0])
+        np.testing.assert_array_equal(g2[:, 3], g3[:, 0])
+    finally:
+        s3.close()
