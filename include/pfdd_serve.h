@@ -21,6 +21,15 @@
  *
  * Stresses follow the ramp of the workloads: step s (0-based) of a solve
  * applies tau_max[a] * ((s + 1.0) / steps).
+ *
+ * Scheduling: free slots take the class's shortest queued solve first; class
+ * streams get CUDA priorities by the size of one solve's step (grid points x
+ * systems), smaller solves more urgent.  Environment switches read at
+ * pfdd_server_create: PFDD_SERVER_TRACE=<file> writes one CSV line per
+ * scheduling event (class creation, admission, chunk, finish, release) when
+ * the server is destroyed; PFDD_SERVER_EXCLUSIVE=1 lets one class's chunk
+ * run on the GPU at a time, most urgent class first (measured slower on the
+ * mixed workloads; off by default).
  */
 #ifndef PFDD_SERVE_H
 #define PFDD_SERVE_H
