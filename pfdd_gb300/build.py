@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
 
 CU_SOURCES = ["pfdd_api.cu", "pfdd_fftpass.cu", "pfdd_zpass.cu", "pfdd_xpass_f32.cu", "pfdd_xpass_f64.cu", "pfdd_xpass_f32b.cu",
-              "pfdd_xpass_warp.cu", "pfdd_xpass_pipe.cu", "pfdd_noalloc.cu"]
+              "pfdd_xpass_warp.cu", "pfdd_noalloc.cu"]
 C_SOURCES = ["pfdd_setup.c"]
 CXX_SOURCES = ["pfdd_server.cpp"]  # host-only C++ (serving scheduler)
 

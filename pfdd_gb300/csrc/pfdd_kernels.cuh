@@ -879,171 +879,6 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   }
 }
 
-// Shared-memory bytes of the pipelined x-pass (tile table, T = 2): twiddles |
-// one tile's lines | one B block of at most ns(ns+1)/2 rows of L + 4 (the same
-// as x_warp_kernel's line-pair tile).
-__host__ __device__ __forceinline__ size_t xp_smem(int ns, int lgL) { return xw_smem(ns, lgL, 1, 4, true); }
-
-// Fused x-pass on the mirrored B(k) tile table (FP32 stored-table form, T = 2,
-// N1 = 32..256), persistent and pipelined: each CTA runs a sequence of work
-// items (replica, tile) and brings the next one's data towards the SM while it
-// computes the current one.  Per item the arithmetic is x_warp_kernel's (same
-// FFT stages, same contraction, same results bit for bit); what changes is how
-// the data arrive:
-//   - when item k starts, its CTA asks the TMA engine to prefetch item k + 1's
-//     lines and B block into L2 (no shared memory held for them), so item
-//     k + 1's own copies come from L2, not HBM;
-//   - the tile's lines (ns * 2 of N1 contiguous values in the x-fastest S)
-//     come by TMA bulk copies, one per line, issued as soon as item k has
-//     written its results; the B block (one contiguous range of the table)
-//     by bulk copies issued right after item k's contraction, so it lands
-//     during item k's inverse FFT.
-// The shared memory is x_warp_kernel's (one line-pair tile and one B block);
-// two CTAs of 256 threads run per SM.  Every wait is bounded; a wait that runs out stops
-// the CTA, which first lets its copies in flight land (again bounded) and
-// reports the timeout in p.err.
-template <int NS, int LG>
-__global__ void __launch_bounds__(256, 2) x_pipe_kernel(XParams p) {
-  using V = float2;
-  static_assert(LG >= 5 && LG <= 8, "the pipelined x-pass covers N1 = 32..256");
-  constexpr int L = 1 << LG, P = NS * (NS + 1) / 2, TT = 2, lines = NS * TT;
-  constexpr int NV = xpass_nv(LG, 8), LV = L / NV, LPW = 32 / LV, LP = xw_pitch(LG);
-  extern __shared__ __align__(16) unsigned char smraw[];
-  V *const tws0 = reinterpret_cast<V *>(smraw);
-  V *const cur0 = tws0 + L;
-  float *Bs = reinterpret_cast<float *>(smraw + ((((size_t)L + (size_t)lines * LP) * sizeof(V) + 15) & ~(size_t)15));
-  __shared__ __align__(8) uint64_t bar_s, bar_b;
-  __shared__ int s_ok;
-  const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
-  const int th = lane & (LV - 1), wl = lane / LV;
-  const long long total = (long long)p.R * p.tiles;
-  const int fstride = (int)p.inner * L;
-  // work item w: replica w % R, tile w / R (a tile's replicas run back to back,
-  // so its B block comes from HBM once and then from L2)
-  struct Item {
-    int2 tp;
-    long long boff;
-    int bvals, tl, W;
-    V *Sr;
-  };
-  auto item = [&](long long w) {
-    Item it;
-    const long long r = w % p.R, tile = w / p.R;
-    it.tp = p.xt[tile];
-    it.boff = p.xtoff[tile];
-    it.bvals = (int)(p.xtoff[tile + 1] - it.boff);
-    it.tl = it.tp.y < 0 ? 1 : TT;
-    it.W = it.tp.y >= 0 ? b_wm(L) : it.bvals / P;
-    it.Sr = reinterpret_cast<V *>(p.S) + r * NS * p.inner * L;
-    return it;
-  };
-  auto goff = [&](const Item &it, int ln) { return (ln >> 1) * fstride + ((ln & 1) ? it.tp.y : it.tp.x) * L; };
-  auto issue_lines = [&](const Item &it) {  // one thread
-    mbar_arrive_expect_tx(&bar_s, (unsigned)(NS * it.tl * L * (int)sizeof(V)));
-    for (int ln = 0; ln < lines; ++ln)
-      if ((ln & 1) < it.tl) bulk_copy(cur0 + ln * LP, it.Sr + goff(it, ln), (unsigned)(L * sizeof(V)), &bar_s);
-  };
-  auto issue_b = [&](const Item &it, bool drop) {  // one thread
-    if (drop) mbar_arrive_expect_tx(&bar_b, (unsigned)(it.bvals * 4));  // failure test: bytes that never come
-    else bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + it.boff, (unsigned)(it.bvals * 4), &bar_b);
-  };
-  auto prefetch = [&](const Item &it) {  // one thread
-    for (int ln = 0; ln < lines; ++ln)
-      if ((ln & 1) < it.tl) bulk_prefetch_l2(it.Sr + goff(it, ln), (unsigned)(L * sizeof(V)));
-    bulk_prefetch_l2(reinterpret_cast<const float *>(p.B) + it.boff, (unsigned)(it.bvals * 4));
-  };
-  long long w = blockIdx.x;
-  if (tid == 0) {
-    mbar_init(&bar_s, 1);
-    mbar_init(&bar_b, 1);
-    s_ok = 1;
-    if (w < total) issue_b(item(w), p.drop_bulk && blockIdx.x == 0);  // B(k) is constant: before the wait
-  }
-  load_twiddles(tws0, reinterpret_cast<const V *>(p.tw), L);
-  griddep_wait();  // S and the step counter come from the kernels before this one
-  if (p.step_ctr && blockIdx.x == 0 && tid == 0) *p.step_ctr += 1;
-  if (tid == 0 && w < total) issue_lines(item(w));
-  __syncthreads();  // barriers initialised, twiddles loaded
-  // Item fields are re-read from the tile table in each phase (cheap cached
-  // loads) rather than kept live across the FFTs, which need the registers.
-  int k = 0;
-#pragma unroll 1
-  for (; w < total; ++k, w += gridDim.x) {
-    const long long wn = w + gridDim.x;
-    V *const cur = cur0;
-    const V *const tws = tws0;
-    if (tid == 0 && wn < total) prefetch(item(wn));
-    bool ok = mbar_wait(&bar_s, (unsigned)(k & 1), p.err, p.wait_ns);
-    // forward FFT of the tile's lines, in place; each line's lanes sit in one
-    // warp and read their values in natural order before the first stage
-    // writes the line back in the swizzled order of the later stages
-    {
-      const int tl = p.xt[w / p.R].y < 0 ? 1 : TT;
-      for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
-        const int ln = ln0 + wl;
-        const bool act = ln < lines && (ln & 1) < tl;
-        V *line = cur + ln * LP;
-        V v[NV];
-        if (act) {
-#pragma unroll
-          for (int m = 0; m < NV; ++m) v[m] = line[th + m * LV];
-        }
-        __syncwarp();
-        line_fft_io<-1, LG, true, false, NV, true>(v, th, tws, [&](int l) { return &line[xw_swz(l, LG)]; },
-                                                   [&](int l) { return &line[xw_swz(l, LG)]; }, act);
-      }
-    }
-    ok = mbar_wait(&bar_b, (unsigned)(k & 1), p.err, p.wait_ns) && ok;
-    if (!ok) s_ok = 0;
-    __syncthreads();
-    if (!s_ok) break;  // uniform: every thread sees the flag after the barrier
-    {
-      const Item it = item(w);
-      for (int q = tid; q < (it.tl << LG); q += nthr) {
-        const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
-        V *const pt = cur + t * LP + sx;  // the point's value of field a at pt[a * 2 * LP]
-        const int bx = t == 0 ? x : (x == L / 2 ? L : b_mirror(x, L));
-        auto table = [&](auto wc) {
-          constexpr int WC = decltype(wc)::value;
-          contract_table<float, NS, true, WC>(Bs, it.W, bx, [&](int a) -> V & { return pt[a * TT * LP]; });
-        };
-        if (it.tl == TT) table(std::integral_constant<int, b_wm(L)>{});
-        else if (it.W == L) table(std::integral_constant<int, L>{});
-        else contract_table<float, NS, true>(Bs, it.W, bx, [&](int a) -> V & { return pt[a * TT * LP]; });
-      }
-    }
-    __syncthreads();  // the B block is free
-    if (tid == 0 && wn < total) {
-      fence_proxy_async_smem();
-      issue_b(item(wn), false);
-    }
-    {
-      const Item it = item(w);
-      for (int ln0 = warp * LPW; ln0 < lines; ln0 += nwarps * LPW) {
-        const int ln = ln0 + wl;
-        const bool act = ln < lines && (ln & 1) < it.tl;
-        V *line = cur + ln * LP;
-        V *g = it.Sr + (act ? goff(it, ln) : 0);
-        V v[NV];
-        line_fft_io<+1, LG, false, true, NV, true>(v, th, tws, [&](int l) { return &line[xw_swz(l, LG)]; },
-                                                   [&](int l) { return &g[l]; }, act);
-      }
-    }
-    __syncthreads();  // the line buffer is free
-    if (tid == 0 && wn < total) {
-      fence_proxy_async_smem();
-      issue_lines(item(wn));
-    }
-  }
-  if (tid == 0 && !s_ok) {
-    // a wait ran out in item k, before anything was issued for item k + 1: the
-    // last phase issued on each barrier is item k's; let its copies land
-    // (bounded) before the CTA exits
-    mbar_wait(&bar_s, (unsigned)(k & 1), nullptr, p.wait_ns);
-    mbar_wait(&bar_b, (unsigned)(k & 1), nullptr, p.wait_ns);
-  }
-}
-
 // Forward twiddle table w[t] = exp(-2 pi i t / L), t < L (sincospi in FP64).
 template <typename T>
 __global__ void twiddle_kernel(void *tw_, int L) {

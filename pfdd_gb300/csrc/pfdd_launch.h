@@ -31,12 +31,7 @@ cudaError_t launch_x_fused_f32_bfly(int ns, unsigned blocks, int threads, size_t
 // warp-team FP32 x-pass (stored or register-evaluated B(k)), N1 in [32, 256]
 cudaError_t launch_x_warp_f32(int ns, bool bfly, unsigned blocks, int threads, size_t smem, cudaStream_t st,
                               const XParams &p);
-// persistent pipelined FP32 x-pass on the B(k) tile table (T = 2), N1 in
-// [32, 256]: `items` work items (replica, tile) over as many CTAs as fit the
-// device at once
-cudaError_t launch_x_pipe_f32(int ns, long long items, int threads, size_t smem, cudaStream_t st, const XParams &p);
-// multiprocessor count of the current device (read once per device)
-cudaError_t device_sm_count(int *out);
+
 
 // Launch geometry of the z-pass, the strided passes and the fused x-pass for one
 // grid (ns = 0: FFT-boundary plans without the x-pass).  Sizes: powers of two <= 512.
@@ -81,11 +76,10 @@ struct Geometry {
   int lgTI[2] = {0, 0}, threads[2] = {1, 1}, pitch[2] = {1, 1}, nv[2] = {0, 0};
   long long tiles[2] = {1, 1};
   size_t smem[2] = {0, 0};
-  // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel); xPipe: its
-  // persistent pipelined form (x_pipe_kernel); xTable: the B(k) tile-table
-  // layout (see BLayout), xTiles then the table's tile count
+  // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel); xTable: the
+  // B(k) tile-table layout (see BLayout), xTiles then the table's tile count
   int xLgT = 0, xPitch = 1, xThreads = 256;
-  bool xWide = false, xWarp = false, xPipe = false, xTable = false;
+  bool xWide = false, xWarp = false, xTable = false;
   long long xTiles = 1;
   size_t xSmem = 0;
 };
@@ -144,34 +138,11 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
 // at the price of idle threads when the tile has fewer lines.
 // table_tiles > 0: the tile-table layout with that many tiles (T = 2: a CTA
 // per tile, T = 1: a CTA per line).
-// pipe: the persistent pipelined form of the warp-team kernel (tile table with
-// line pairs only, T = 2).
 inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT,
-                           bool wide = false, bool warp = false, long long table_tiles = 0, bool pipe = false) {
+                           bool wide = false, bool warp = false, long long table_tiles = 0) {
   const long long innerx = (long long)n2 * n3;
   if ((1LL << lgT) > innerx && table_tiles == 0) return false;
   if (table_tiles > 0 && lgT > 1) return false;
-  if (pipe) {  // FP32 spectra, N1 = 32..256, stored B(k) in the tile table, line pairs
-    const int lgL = ilog2(n1);
-    if (wide || !warp || vsize != 8 || bsize != 4 || n1 < 32 || n1 > 256 || table_tiles <= 0 || lgT != 1)
-      return false;
-    const size_t smem = xp_smem(ns, lgL);
-    if (smem > kMaxDynSmem) return false;
-    const int lpw = 32 / xw_lv(lgL), lines = ns << 1;
-    int thr = std::max(n1 << 1, (lines + lpw - 1) / lpw * 32);
-    thr = std::min(256, (thr + 31) / 32 * 32);  // x_pipe_kernel launch bounds
-    g.xPitch = xw_pitch(lgL);
-    g.xLgT = 1;
-    g.xTiles = table_tiles;
-    g.xSmem = smem;
-    g.xThreads = thr;
-    g.xWide = false;
-    g.xWarp = true;
-    g.xPipe = true;
-    g.xTable = true;
-    return true;
-  }
-  g.xPipe = false;
   if (warp) {  // FP32 spectra, N1 = 32..256; a thread a point, at most 384
     const int lgL = ilog2(n1);
     if (wide || vsize != 8 || n1 < 32 || n1 > 256) return false;

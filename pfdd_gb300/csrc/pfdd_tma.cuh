@@ -103,22 +103,6 @@ __device__ __forceinline__ void bulk_load_evict_first(void *dst, const void *src
   }
 }
 
-// One thread: asks the TMA engine to bring `bytes` (multiple of 16, address
-// 16-byte aligned) of global memory into L2, without waiting.
-__device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes) {
-  for (unsigned off = 0; off < bytes; off += kBulkChunk) {
-    const unsigned n = bytes - off < kBulkChunk ? bytes - off : kBulkChunk;
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char *)src + off), "r"(n) : "memory");
-  }
-}
-
-// Orders this thread's earlier shared-memory accesses through the generic
-// proxy (ordinary loads and stores, made visible to it by a block barrier)
-// before its later bulk copies (async proxy) into the same shared memory.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
 // Programmatic dependent launch (kernels launched with launch_pdl): a kernel
 // may be launched while the previous kernel on its stream finishes, does the
 // work that does not depend on it (constant tables, TMA copies of data written

@@ -180,34 +180,6 @@ def test_y_field_order_same_bits(native_lib, precision):
         np.testing.assert_array_equal(x1, x0)
 
 
-@pytest.mark.parametrize("n", [(128, 8, 16), (32, 16, 8), (64, 4, 2), (256, 4, 8), (128, 128, 4)])
-def test_pipelined_xpass_gives_same_bits(native_lib, n):
-    """The persistent pipelined x-pass (each CTA prefetches its next work item's
-    lines and B block into L2 and copies them in by TMA while the current one
-    computes) gives the warp-team kernel's bits on the mirrored B(k) tile table,
-    including the single-line tiles of the Nyquist lines, for one solve and for
-    a batch with an idle replica and pinned points."""
-    w = 2
-    spec = workloads.SolveSpec(n=n, ns=12, steps=6, sigma_max=0.05, noise_seed=37,
-                               loops=workloads.random_loops(n, 2, 1.0, 3.0, 12, seed=37))
-    g1, x1, p1 = pinned(spec, "fp32", f"x=2,w={w}")
-    g0, x0, p0 = pinned(spec, "fp32", "x=2,w=1")
-    assert p1["x_pass"]["pipelined"] == 1 and p0["x_pass"]["pipelined"] == 0
-    assert p1["x_pass"]["warp_teams"] == 1 and p1["x_pass"]["b_mirrored"] == 1
-    np.testing.assert_array_equal(g1, g0)
-    np.testing.assert_array_equal(x1, x0)
-
-    def prep(s, b0):
-        bc = np.zeros((3,) + b0.shape); bc[:, :, 0, 0, :] = 1.0
-        s.set_state(s.get_state(), bc)
-        s.set_active(1, False)
-
-    res = [pinned(spec, "fp32", plan, nrep=3, prepare=prep) for plan in (f"x=2,w={w}", "x=2,w=1")]
-    live = [0, 2]
-    np.testing.assert_array_equal(res[0][0][:, live], res[1][0][:, live])
-    np.testing.assert_array_equal(res[0][1], res[1][1])
-
-
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_every_radix_plan_matches_oracle(native_lib, precision):
     """The z-pass and y-pass radix plans the autotuner chooses from (8 or 16
