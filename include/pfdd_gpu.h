@@ -118,6 +118,32 @@ pfdd_status pfdd_set_tau_field(pfdd_ctx *ctx, const double *tau_field);
  * gamma_a[nsteps][nrep][ns] (per system, F:3495). */
 pfdd_status pfdd_step(pfdd_ctx *ctx, int nsteps, const double *tau, double *gamma, double *gamma_a);
 
+/* The inner loop's convergence stop (plasticconverge, F:3732-3785, applied by
+ * the do-while at F:4574-4691), for a one-solve context (nrep == 1).
+ *
+ * pfdd_converge_reset starts an inner loop (F:4567-4572): it clears the
+ * per-step pass marks and the count of full windows; gamma_prev is the gamma
+ * the loop's first step is compared with (the last gamma of the previous
+ * loop, 0.0 before the first, F:4192 / F:4575).
+ *
+ * pfdd_step_converge then runs up to max_steps steps like pfdd_step and stops
+ * after the step at which the reference leaves the loop: a step passes when
+ * |(gamma - gamma_last) / gamma| < 1e-8 or |gamma| < 1e-12 (for gamma == 0:
+ * |gamma - gamma_last| < 1e-15 or |gamma| < 1e-14); once 30 steps in a row
+ * have passed, each further passing step with a full window counts, a
+ * passing step whose window is not full resets the count, and the loop ends
+ * at the fifth count.  tau[max_steps][ns] as for pfdd_step; gamma[max_steps]
+ * and gamma_a[max_steps][ns] (may be NULL) receive the steps that ran;
+ * *steps_done = how many (== max_steps when the loop did not converge).  The
+ * pass marks carry over between calls, so a loop may be run in pieces.  The
+ * state after the call is the state after the last step that ran: steps run
+ * in chunks, and a chunk that ran past the stop is rewound (a device copy of
+ * xi taken at its start) and run again up to the stop, which gives the same
+ * bits. */
+pfdd_status pfdd_converge_reset(pfdd_ctx *ctx, double gamma_prev);
+pfdd_status pfdd_step_converge(pfdd_ctx *ctx, int max_steps, const double *tau, double *gamma, double *gamma_a,
+                               int *steps_done);
+
 /* Copies xi of every replica back: xi[nrep][ns][N][2]. */
 pfdd_status pfdd_get_state(pfdd_ctx *ctx, double *xi);
 pfdd_status pfdd_get_replica_state(pfdd_ctx *ctx, int r, double *xi);

@@ -142,6 +142,34 @@ def solve(spec, steps: int | None = None, eps_bdiv: float = float(np.sqrt(2.0)))
     return run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf), np.full(ns, spec.dslip), 1.0, tau)
 
 
+def converge_stop(gamma: np.ndarray, gamma_prev: float = 0.0) -> int | None:
+    """The inner loop's stop (plasticconverge, F:3732-3785, under the do-while of
+    F:4574-4691) on a sequence of per-step gammas: the number of steps the
+    reference runs, or None when it would run them all.  A step passes when
+    |(g - g_last) / g| < 1e-8 or |g| < 1e-12 (g == 0: |g - g_last| < 1e-15 or
+    |g| < 1e-14); a passing step from index 29 on adds one to the count when
+    the last 30 steps all passed and otherwise resets it; the loop ends at a
+    count of 5.  g_last of the first step is ``gamma_prev`` (F:4575)."""
+    passed = np.zeros(len(gamma), dtype=bool)
+    count, last = 0, float(gamma_prev)
+    for it, g in enumerate(map(float, gamma)):
+        if g != 0:
+            ok = abs((g - last) / g) < 1e-8 or abs(g) < 1e-12
+        else:
+            ok = abs(g - last) < 1e-15 or abs(g) < 1e-14
+        if ok:
+            passed[it] = True
+            if it >= 29:
+                if passed[it - 29:it + 1].all():
+                    count += 1
+                elif count != 0:
+                    count = 0
+        if count == 5:
+            return it + 1
+        last = g
+    return None
+
+
 def strain_stress(n, xi: np.ndarray, eps: np.ndarray, C11: float, C12: float, C44: float, sigma_app: np.ndarray,
                   d=(1.0, 1.0, 1.0)):
     """Strain and stress fields of state ``xi`` (complex [ns, n1, n2, n3]):

@@ -440,6 +440,14 @@ struct pfdd_ctx {
   double *d_dgat = nullptr;
   std::vector<double> h_dgat, h_diag;
   int diag_steps = 0;
+  // the inner loop's convergence stop (plasticconverge, F:3732-3785): which
+  // steps of the current loop passed the change test, the run of full 30-step
+  // windows, the loop's step count and the previous gamma; and a copy of xi
+  // to rewind a chunk that ran past the stop (pfdd_step_converge)
+  std::vector<uint8_t> cv_test;
+  int cv_count = 0, cv_it = 0;
+  double cv_last = 0.0;
+  double2 *xi_snap = nullptr;
 };
 
 // wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
@@ -716,7 +724,7 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
                 c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2],
                 c->xt, c->xtoff, c->xline, c->xord, c->sp_E, c->sp_eps, c->sp_sig, c->sp_part, c->sp_dp,
-                c->d_dpts, c->d_dgat};
+                c->d_dpts, c->d_dgat, c->xi_snap};
   if (c->sp_plan) pfdd_fft_plan_destroy(c->sp_plan);
   if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
@@ -1494,6 +1502,92 @@ extern "C" pfdd_status pfdd_step(pfdd_ctx *c, int nsteps, const double *tau, dou
   CK(c, cudaSetDevice(c->dev));
   return c->prec == PFDD_FP64 ? run_steps<double>(c, nsteps, tau, gamma, gamma_a)
                               : run_steps<float>(c, nsteps, tau, gamma, gamma_a);
+}
+
+// plasticconverge (F:3732-3785) for the gamma of one more step of the inner
+// loop: the step passes when gamma changed by less than 1e-8 relative (1e-15
+// absolute when gamma is 0) or |gamma| < 1e-12 (1e-14); a passing step whose
+// last 30 steps all passed extends the run of full windows, one whose window
+// is not full resets it (a failing step leaves it); the loop stops when the
+// run reaches 5.  True: the loop stops after this step.
+static bool converge_update(pfdd_ctx *c, double g) {
+  const double gl = c->cv_last;
+  bool passed;
+  if (g != 0) {
+    const double r = (g - gl) / g;
+    passed = (r < 0 ? -r : r) < 1E-8 || (g > 0 ? g : -g) < 1E-12;
+  } else {
+    const double d = g - gl;
+    passed = (d < 0 ? -d : d) < 1E-15 || (g > 0 ? g : -g) < 1E-14;
+  }
+  const int it = c->cv_it;
+  if ((int)c->cv_test.size() <= it) c->cv_test.resize((size_t)it + 1, 0);
+  if (passed) {
+    c->cv_test[it] = 1;
+    if (it >= 29) {
+      int t = 0;
+      for (int i = 0; i < 30; ++i) t += c->cv_test[it - i];
+      if (t == 30) c->cv_count++;
+      else if (c->cv_count != 0) c->cv_count = 0;
+    }
+  }
+  bool stop = false;
+  if (c->cv_count == 5) {
+    c->cv_count++;
+    stop = true;
+  }
+  c->cv_last = g;
+  c->cv_it++;
+  return stop;
+}
+
+extern "C" pfdd_status pfdd_converge_reset(pfdd_ctx *c, double gamma_prev) {
+  if (!c) return PFDD_EINVAL;
+  c->cv_test.clear();
+  c->cv_count = 0;
+  c->cv_it = 0;
+  c->cv_last = gamma_prev;
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_step_converge(pfdd_ctx *c, int max_steps, const double *tau, double *gamma,
+                                          double *gamma_a, int *steps_done) {
+  if (!c || max_steps < 0 || (max_steps > 0 && (!tau || !gamma)) || !steps_done)
+    return fail(c, PFDD_EINVAL, "pfdd_step_converge: bad argument");
+  if (c->nrep != 1) return fail(c, PFDD_EINVAL, "pfdd_step_converge: one solve per context (nrep == 1)");
+  *steps_done = 0;
+  if (max_steps == 0) return PFDD_OK;
+  if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_step_converge: state not set");
+  CK(c, cudaSetDevice(c->dev));
+  const size_t xbytes = (size_t)c->ns * c->N * sizeof(double2);
+  if (!c->xi_snap) CK(c, cudaMalloc(&c->xi_snap, xbytes));
+  const int ns = c->ns;
+  std::vector<double> ga_tmp;
+  int done = 0;
+  while (done < max_steps) {
+    const int k = std::min(c->kchunk, max_steps - done);
+    CK(c, cudaMemcpyAsync(c->xi_snap, c->xi, xbytes, cudaMemcpyDeviceToDevice, c->st));
+    double *ga = gamma_a ? gamma_a + (size_t)done * ns : nullptr;
+    pfdd_status st = pfdd_step(c, k, tau + (size_t)done * ns, gamma + done, ga);
+    if (st != PFDD_OK) return st;
+    int stop = -1;
+    for (int j = 0; j < k && stop < 0; ++j)
+      if (converge_update(c, gamma[done + j])) stop = j;
+    if (stop < 0) {
+      done += k;
+      continue;
+    }
+    if (stop < k - 1) {  // rewind to the chunk's start and run exactly to the stop (same bits)
+      CK(c, cudaMemcpyAsync(c->xi, c->xi_snap, xbytes, cudaMemcpyDeviceToDevice, c->st));
+      c->specValid = false;
+      st = pfdd_step(c, stop + 1, tau + (size_t)done * ns, gamma + done, ga);
+      if (st != PFDD_OK) return st;
+    }
+    done += stop + 1;
+    break;
+  }
+  *steps_done = done;
+  return PFDD_OK;
 }
 
 extern "C" pfdd_status pfdd_get_plan(pfdd_ctx *c, char *buf, size_t len) {

@@ -12,11 +12,13 @@
  * writes strain.txt (F:818-831) and stress.txt (F:927-944) of the state it
  * starts from, and stress-strain.dat (F:4063-4072, 4694-4698): the grid means
  * of strain and stress (over C44) of the starting state and of the final
- * state, then the final gamma_a and gamma.
+ * state, then the final gamma_a and gamma.  With --converge the loop stops
+ * where the reference's convergence test ends it (plasticconverge,
+ * F:3732-3785) and the files hold the steps that ran.
  *
  * usage: pfdd_run N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C]
  *                 [--mu MU] [--lambda LAM] [--bdiv BD] [--fp32] [--device D]
- *                 [--strain]
+ *                 [--strain] [--converge]
  *
  * NSF (default NS) is the slip-system count of the files; systems NS..NSF-1
  * and the 9 virtual-strain fields must be zero and pinned (they contribute
@@ -74,12 +76,12 @@ static int write_fields(int n1, int n2, int n3, const double *e, const double *s
 int main(int argc, char **argv) {
   if (argc < 7) {
     fprintf(stderr, "usage: %s N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C] [--mu MU] [--lambda LAM] "
-                    "[--bdiv BD] [--fp32] [--device D] [--strain]\n", argv[0]);
+                    "[--bdiv BD] [--fp32] [--device D] [--strain] [--converge]\n", argv[0]);
     return 2;
   }
   int n1 = atoi(argv[1]), n2 = atoi(argv[2]), n3 = atoi(argv[3]), ns = atoi(argv[4]), K = atoi(argv[5]);
   double sigma_max = atof(argv[6]);
-  int nsf = ns, prec = PFDD_FP64, dev = 0, strain = 0;
+  int nsf = ns, prec = PFDD_FP64, dev = 0, strain = 0, conv = 0;
   double asf = 0.1, cd2 = 0.01, mu = 1.0, lam = 1.5, bdiv = sqrt(2.0);
   for (int i = 7; i < argc; ++i) {
     if (!strcmp(argv[i], "--nsfile") && i + 1 < argc) nsf = atoi(argv[++i]);
@@ -91,6 +93,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[i], "--fp32")) prec = PFDD_FFT_FP32;
     else if (!strcmp(argv[i], "--device") && i + 1 < argc) dev = atoi(argv[++i]);
     else if (!strcmp(argv[i], "--strain")) strain = 1;
+    else if (!strcmp(argv[i], "--converge")) conv = 1;
     else { fprintf(stderr, "unknown option %s\n", argv[i]); return 2; }
   }
   if (ns < 1 || ns > 12 || nsf < ns || K < 1) { fprintf(stderr, "bad NS/K\n"); return 2; }
@@ -142,12 +145,18 @@ int main(int argc, char **argv) {
     free(e); free(sg);
   }
   double t1 = wtime();
-  if ((st = pfdd_step(c, K, tau, gamma, gamma_a)) != PFDD_OK) return die("step", c, st);
+  int Kr = K; /* steps that ran */
+  if (!conv) {
+    if ((st = pfdd_step(c, K, tau, gamma, gamma_a)) != PFDD_OK) return die("step", c, st);
+  } else {
+    if ((st = pfdd_converge_reset(c, 0.0)) != PFDD_OK) return die("converge_reset", c, st);
+    if ((st = pfdd_step_converge(c, K, tau, gamma, gamma_a, &Kr)) != PFDD_OK) return die("step_converge", c, st);
+  }
   double t2 = wtime();
   if ((st = pfdd_get_state(c, xi)) != PFDD_OK) return die("get_state", c, st);
 
   FILE *pf = fopen("phasefield.dat", "w"), *gf = fopen("gamma_full.dat", "w");
-  for (int s = 0; s < K; ++s) {
+  for (int s = 0; s < Kr; ++s) {
     /* it = 1: the single outer step that runs the inner loop; it_plastic counts from 1 */
     fprintf(pf, "%d       %d         %e           %e           %e\n", 1, s + 1, gamma_a[(size_t)s * ns],
             ns > 1 ? gamma_a[(size_t)s * ns + 1] : 0.0, gamma[s]);
@@ -162,15 +171,15 @@ int main(int argc, char **argv) {
     if (!f2) { fprintf(stderr, "cannot write stress-strain.dat\n"); return 1; }
     for (int q = 0; q < 9; ++q) fprintf(f2, "%e %e ", ave0[0][q], ave0[1][q] / C44);
     for (int q = 0; q < 9; ++q) fprintf(f2, "%e %e ", ave1[0][q], ave1[1][q] / C44);
-    for (int a = 0; a < nsf; ++a) fprintf(f2, "\t%e", a < ns ? gamma_a[(size_t)(K - 1) * ns + a] : 0.0);
-    fprintf(f2, " %e \n", gamma[K - 1]);
+    for (int a = 0; a < nsf; ++a) fprintf(f2, "\t%e", a < ns ? gamma_a[(size_t)(Kr - 1) * ns + a] : 0.0);
+    fprintf(f2, " %e \n", gamma[Kr - 1]);
     fclose(f2);
   }
   FILE *fo = fopen("xi.dat", "r+b");
   if (!fo || fwrite(xi, sizeof(double), cnt, fo) != cnt) { fprintf(stderr, "cannot write xi.dat\n"); return 1; }
   fclose(fo);
-  printf("pfdd_run: %dx%dx%d ns=%d K=%d %s setup %.3fs steps %.3fs (%.1f steps/s)\n", n1, n2, n3, ns, K,
-         prec == PFDD_FP64 ? "fp64" : "fp32", t1 - t0, t2 - t1, K / (t2 - t1));
+  printf("pfdd_run: %dx%dx%d ns=%d K=%d of %d %s setup %.3fs steps %.3fs (%.1f steps/s)\n", n1, n2, n3, ns, Kr, K,
+         prec == PFDD_FP64 ? "fp64" : "fp32", t1 - t0, t2 - t1, Kr / (t2 - t1));
   pfdd_destroy(c);
   free(xi); free(bc); free(tau); free(gamma); free(gamma_a);
   return 0;

@@ -33,6 +33,7 @@ EXPORTS = [
     "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
     "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority", "pfdd_get_plan",
     "pfdd_strain_stress", "pfdd_set_diagnostics", "pfdd_get_diagnostics", "pfdd_state_diagnostics",
+    "pfdd_converge_reset", "pfdd_step_converge",
 ]
 
 DIAG_COLUMNS = ("energy_in", "energy_in2", "energy_in3", "energy_in4", "energy_Residual", "energy_intotal")
@@ -97,6 +98,8 @@ def load():
     L.pfdd_set_replica_state.argtypes = [vp, i, dp, dp]
     L.pfdd_set_tau_field.argtypes = [vp, dp]
     L.pfdd_step.argtypes = [vp, i, dp, dp, dp]
+    L.pfdd_converge_reset.argtypes = [vp, d]
+    L.pfdd_step_converge.argtypes = [vp, i, dp, dp, dp, C.POINTER(C.c_int)]
     L.pfdd_get_state.argtypes = [vp, dp]
     L.pfdd_get_replica_state.argtypes = [vp, i, dp]
     L.pfdd_set_replica_active.argtypes = [vp, i, i]
@@ -272,6 +275,23 @@ class Solver:
         g = np.zeros((K, self.nrep)); ga = np.zeros((K, self.nrep, self.ns))
         self._check(self.L.pfdd_step(self.h, K, _dp(t), _dp(g), _dp(ga)), "pfdd_step")
         return g, ga
+
+    def converge_reset(self, gamma_prev: float = 0.0):
+        """Starts an inner loop for step_converge (F:4567-4572); gamma_prev is
+        the gamma its first step is compared with (F:4575)."""
+        self._check(self.L.pfdd_converge_reset(self.h, float(gamma_prev)), "pfdd_converge_reset")
+
+    def step_converge(self, tau: np.ndarray):
+        """Runs at most len(tau) steps (tau [K, ns]; nrep == 1) and stops where
+        the reference's convergence test (plasticconverge, F:3732-3785) ends the
+        inner loop.  Returns gamma [k] and gamma_a [k, ns] of the k steps run."""
+        t = _f64(np.asarray(tau).reshape(-1, self.ns))
+        K = t.shape[0]
+        g = np.zeros(K); ga = np.zeros((K, self.ns)); done = C.c_int(0)
+        self._check(self.L.pfdd_step_converge(self.h, K, _dp(t), _dp(g), _dp(ga), C.byref(done)),
+                    "pfdd_step_converge")
+        k = done.value
+        return g[:k].copy(), ga[:k].copy()
 
     def get_state(self) -> np.ndarray:
         x = np.zeros((self.nrep, self.ns, self.N, 2))

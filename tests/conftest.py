@@ -26,7 +26,7 @@ def native_lib():
 
 def golden_cases():
     """Trajectory cases (gamma per step and final xi of the reference's own run)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("strain_", "oracle_", "diag_")))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("strain_", "oracle_", "diag_", "converge_")))
 
 
 def diag_golden_cases():

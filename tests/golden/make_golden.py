@@ -138,6 +138,25 @@ def make_oracle_long(name: str = "oracle_config1_128c_ns12_k1000", every: int = 
     np.savez_compressed(OUT / f"{name}.npz", **out)
 
 
+def converge_cases():
+    """Solves the reference stops early by its convergence test (plasticconverge,
+    F:3732-3785): noise relaxing under no stress with the reference's own
+    kinetic coefficient CD2 = 0.1; K = 300 steps allowed."""
+    yield "converge_16c_ns3_cd01", workloads.SolveSpec(n=(16, 16, 16), ns=3, steps=300, sigma_max=0.0,
+                                                       noise_seed=5, cd2=0.1)
+
+
+def make_converge(name: str, spec: workloads.SolveSpec):
+    g, x = run_case(name, spec, True)
+    out = dict(spec=spec_json(spec), steps_run=np.array(g.shape[0]), gamma=g[:, 1], gamma_a=g[:, 2:2 + spec.ns],
+               xi_final=x.reshape(spec.ns, -1),
+               xi_final_checksum=np.array([x.real.sum(), x.imag.sum(), (np.abs(x) ** 2).sum()]))
+    xi0, _ = workloads.initial_state(spec)
+    out["xi0_checksum"] = np.array([xi0.real.sum(), (xi0.real ** 2).sum()])
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print(f"{name}: the reference stopped after {g.shape[0]} of {spec.steps} steps")
+
+
 def diag_cases():
     """Interface-plane energy diagnostics (patch 13 of oracle/build_ref.py): the
     reference's full-precision copies of checkEnergy.dat (one line per outer
@@ -232,3 +251,6 @@ if __name__ == "__main__":
     for nm, sp in diag_cases():
         if not want or nm in want:
             make_diag(nm, sp)
+    for nm, sp in converge_cases():
+        if not want or nm in want:
+            make_converge(nm, sp)

@@ -1,0 +1,49 @@
+"""The inner loop's convergence stop (plasticconverge, F:3732-3785): the
+oracle's restatement of the rule, pinned on the reference's own run of a solve
+that stops early (tests/golden/converge_16c_ns3_cd01.npz: the compiled
+reference with its stop left in, 112 of 300 steps).  The GPU test then checks
+pfdd_step_converge against the same golden and this restatement."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import oracle
+
+CASE = "converge_16c_ns3_cd01"
+
+
+def test_restated_rule_stops_where_the_reference_stopped():
+    spec, g = load_golden(CASE)
+    k = int(g["steps_run"])
+    assert k < spec.steps  # the golden is an early stop
+    # on the reference's own gammas: the stop falls on the last step it ran
+    assert oracle.converge_stop(g["gamma"]) == k
+    assert oracle.converge_stop(g["gamma"][:k - 1]) is None
+
+
+def test_oracle_trajectory_stops_at_the_same_step():
+    spec, g = load_golden(CASE)
+    k = int(g["steps_run"])
+    x, gam, ga = oracle.solve(spec)
+    assert oracle.converge_stop(gam) == k
+    np.testing.assert_allclose(gam[:k], g["gamma"], rtol=1e-10, atol=1e-16)
+    np.testing.assert_allclose(ga[:k], g["gamma_a"], rtol=1e-10, atol=1e-16)
+    xk = oracle.solve(spec, steps=k)[0].reshape(spec.ns, -1)
+    assert np.max(np.abs(xk - g["xi_final"])) <= 1e-10 * np.max(np.abs(g["xi_final"]))
+
+
+@pytest.mark.parametrize("seq,prev,want", [
+    # 30 steps of no change from the start: the counts reach 5 at index 33
+    (np.full(40, 1e-3), 1e-3, 34),
+    # gamma zero throughout (the second test form): the same
+    (np.zeros(40), 0.0, 34),
+    # first step fails (gamma jumps from prev), then no change: window full at index 30
+    (np.full(40, 1e-3), 0.0, 35),
+    # a failing step leaves the count alone, and the window keeps it from growing
+    # until 30 passing steps follow it
+    (np.concatenate([np.full(32, 1e-3), [2e-3], np.full(40, 2e-3)]), 1e-3, 33 + 29 + 5),
+    # never converges
+    (np.arange(1, 60) * 1e-3, 0.0, None),
+])
+def test_rule_cases(seq, prev, want):
+    assert oracle.converge_stop(seq, prev) == want

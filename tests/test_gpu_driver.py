@@ -38,3 +38,22 @@ def test_host_driver_fp32_form(native_lib, tmp_path):
     assert r.returncode == 0, r.stderr
     g = np.loadtxt(tmp_path / "gamma_full.dat", ndmin=2)
     np.testing.assert_allclose(g[:, 1], z["gamma"], rtol=1e-5)
+
+
+def test_host_driver_converge_stops_where_the_reference_stopped(native_lib, tmp_path):
+    """--converge: the reference's inner-loop stop (plasticconverge,
+    F:3732-3785); the reference's own run stopped after 112 of 300 steps."""
+    spec, z = load_golden("converge_16c_ns3_cd01")
+    xi, bc = workloads.initial_state(spec)
+    refio.write_xi_files(tmp_path, xi, bc, ns_ref=12)
+    r = subprocess.run([str(build.RUNNER), *map(str, spec.n), str(spec.ns), str(spec.steps), repr(spec.sigma_max),
+                        "--nsfile", "12", "--cd2", repr(spec.cd2), "--converge"], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    k = int(z["steps_run"])
+    g = np.loadtxt(tmp_path / "gamma_full.dat", ndmin=2)
+    assert g.shape[0] == k
+    np.testing.assert_allclose(g[:, 1], z["gamma"], rtol=1e-10, atol=1e-16)
+    assert len((tmp_path / "phasefield.dat").read_text().splitlines()) == k
+    xf = refio.read_xi_file(tmp_path / "xi.dat", spec.n, 21)
+    assert np.max(np.abs(xf[:3].reshape(3, -1) - z["xi_final"])) <= 1e-10 * np.max(np.abs(z["xi_final"]))
