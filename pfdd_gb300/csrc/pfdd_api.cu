@@ -46,7 +46,6 @@ __device__ __forceinline__ double i128_to_double(__int128 v) {
 // exact integers, so neither the split of the partials over lanes nor the
 // order of the additions changes a result.
 constexpr int kGammaWarps = 2;
-constexpr int kMaxGroups = 12;  // slip-system groups of a step (plan)
 
 __device__ __forceinline__ __int128 shfl_down_i128(__int128 v, int o) {
   const unsigned long long lo = __shfl_down_sync(0xffffffffu, (unsigned long long)v, o);
@@ -398,7 +397,7 @@ struct pfdd_ctx {
   // wrote last, which are still in L2 (the x-pass takes every field per tile)
   bool yRev = true;
   BFlyParams bf{};
-  long long launches = 0, graph_launches = 0;
+  long long launches = 0;
   KTiming tm;
   std::string err;
   // step counter on the device (the x-pass advances it, the z-pass reads it),
@@ -449,16 +448,6 @@ struct pfdd_ctx {
   int cv_count = 0, cv_it = 0;
   double cv_last = 0.0;
   double2 *xi_snap = nullptr;
-  // slip-system groups (plan): with G > 1 the y passes run per group on yst
-  // and the z-pass per group on zst, so that one group's y passes (HBM-bound)
-  // overlap another group's z-pass (issue-bound); the x-pass couples every
-  // system and stays on st.  Groups are ranges of systems of one replica
-  // (krep == 1) or ranges of whole replicas.
-  int zgroups = 1;
-  bool seq_fresh = true;
-  cudaStream_t yst = nullptr, zst = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_x = nullptr, ev_y = nullptr, ev_yend = nullptr, ev_zend = nullptr;
-  cudaEvent_t ev_yi[kMaxGroups] = {}, ev_z[kMaxGroups] = {};
 };
 
 // wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
@@ -512,37 +501,6 @@ static void t_end(pfdd_ctx *c, int id) {
   cudaEventRecord(c->tm.pool[c->tm.used + 1], c->st);
   c->tm.ids.push_back(id);
   c->tm.used += 2;
-}
-
-// The two streams and the events of grouped steps, made on first use with
-// the priority of the context's stream.
-static void destroy_aux_streams(pfdd_ctx *c) {
-  if (c->yst) cudaStreamSynchronize(c->yst);
-  if (c->zst) cudaStreamSynchronize(c->zst);
-  for (cudaEvent_t *e : {&c->ev_fork, &c->ev_x, &c->ev_y, &c->ev_yend, &c->ev_zend})
-    if (*e) { cudaEventDestroy(*e); *e = nullptr; }
-  for (int g = 0; g < kMaxGroups; ++g) {
-    if (c->ev_yi[g]) { cudaEventDestroy(c->ev_yi[g]); c->ev_yi[g] = nullptr; }
-    if (c->ev_z[g]) { cudaEventDestroy(c->ev_z[g]); c->ev_z[g] = nullptr; }
-  }
-  if (c->yst) { cudaStreamDestroy(c->yst); c->yst = nullptr; }
-  if (c->zst) { cudaStreamDestroy(c->zst); c->zst = nullptr; }
-}
-
-static cudaError_t ensure_aux_streams(pfdd_ctx *c) {
-  if (c->yst) return cudaSuccess;
-  int prio = 0;
-  cudaError_t e = cudaStreamGetPriority(c->st, &prio);
-  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->yst, cudaStreamNonBlocking, prio);
-  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->zst, cudaStreamNonBlocking, prio);
-  for (cudaEvent_t *ev : {&c->ev_fork, &c->ev_x, &c->ev_y, &c->ev_yend, &c->ev_zend})
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
-  for (int g = 0; g < kMaxGroups && e == cudaSuccess; ++g) {
-    e = cudaEventCreateWithFlags(&c->ev_yi[g], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_z[g], cudaEventDisableTiming);
-  }
-  if (e != cudaSuccess) destroy_aux_streams(c);
-  return e;
 }
 
 // Stockham radices of a line of length n transformed with nv values per
@@ -620,13 +578,6 @@ static cudaError_t make_twiddles(void **tw, const int n[3], int prec, cudaStream
 
 template <typename T>
 static pfdd_status autotune(pfdd_ctx *c);
-template <typename T>
-static cudaError_t launch_step(pfdd_ctx *c, ZParams &zp);
-template <typename T>
-static cudaError_t capture_steps(pfdd_ctx *c, ZParams &zp, int steps, cudaGraphExec_t *out);
-static int step_groups(const pfdd_ctx *c);
-static cudaError_t seq_begin(pfdd_ctx *c);
-static cudaError_t seq_end(pfdd_ctx *c);
 
 // Copies a tile table to the context's device arrays (sized for the single-
 // tile table, the largest) and records its tile count.
@@ -782,7 +733,6 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   if (c->h_gam_a) cudaFreeHost(c->h_gam_a);
   if (c->h_gam) cudaFreeHost(c->h_gam);
   if (c->h_tau) cudaFreeHost(c->h_tau);
-  destroy_aux_streams(c);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1045,67 +995,31 @@ extern "C" pfdd_status pfdd_set_replica_active(pfdd_ctx *c, int r, int on) {
 
 static int prec_code(int prec) { return prec == PFDD_FP64 ? 0 : 1; }
 
-// A range of fields (replica-major index rf = r * ns + a) of one grouped
-// launch: systems [rf0, rf0 + nrf) of replica 0 when krep == 1, otherwise
-// whole replicas.  The kernels see the range as a context of its own through
-// offset pointers (the default: every field of replicas [0, krep)).
-struct FieldRange {
-  int rf0 = 0, nrf = -1;
-};
-
-// The z-pass parameters of a field range: every per-field pointer and
-// per-system coefficient shifted to the range's first field (the kernel's
-// step strides R and ns stay the context's).
-static ZParams zparams_for(const pfdd_ctx *c, const ZParams &zp, int rf0) {
-  ZParams q = zp;
-  if (rf0 == 0) return q;
-  const int r0 = rf0 / c->ns, a0 = rf0 % c->ns;
-  q.S = static_cast<char *>(zp.S) + (size_t)rf0 * c->N * vsize_of(c->prec);
-  q.xi = zp.xi + (size_t)rf0 * c->N;
-  if (zp.bc) q.bc = zp.bc + (size_t)rf0 * c->N / 32;  // grouped steps need N % 32 == 0
-  q.tau = zp.tau + rf0;
-  if (zp.tau_field) q.tau_field = zp.tau_field + (size_t)a0 * c->N;
-  if (zp.dslip) q.dslip = zp.dslip + a0;
-  q.part = zp.part + (size_t)rf0 * zp.nparts;
-  if (zp.active) q.active = zp.active + r0;
-  for (int a = 0; a + a0 < c->ns; ++a) {
-    q.cd2[a] = zp.cd2[a + a0];
-    q.asf_pi[a] = zp.asf_pi[a + a0];
-    q.uq2cd2[a] = zp.uq2cd2[a + a0];
-  }
-  return q;
-}
-
-static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags, FieldRange fr = {}, cudaStream_t st = nullptr) {
+static cudaError_t ctx_zpass(pfdd_ctx *c, ZParams &zp, int flags) {
   zp.flags = flags;
-  const long long nrf = fr.nrf < 0 ? (long long)c->krep * c->ns : fr.nrf;
-  const long long blocks = nrf * c->g.zNparts;
-  const ZParams q = zparams_for(c, zp, fr.rf0);
+  const long long blocks = (long long)c->krep * c->ns * c->g.zNparts;
   t_begin(c);
-  cudaError_t e = launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem,
-                               st ? st : c->st, q, c->g.zNV);
+  cudaError_t e =
+      launch_zpass(prec_code(c->prec), c->g.lgL3, (unsigned)blocks, c->g.zThreads, c->g.zSmem, c->st, zp, c->g.zNV);
   t_end(c, (flags & Z_UPDATE) ? K_Z_STEP : K_Z_PROLOGUE);
   return e;
 }
 
-static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/, FieldRange fr = {},
-                               cudaStream_t st = nullptr) {
+static cudaError_t ctx_strided(pfdd_ctx *c, int sign, int ax /*0: y, 1: x*/) {
   const int L = ax == 0 ? c->n[1] : c->n[0];
   if (L == 1) return cudaSuccess;
   const int gi = ax == 0 ? 0 : 1;
   // y lines: stride N3*N1 in the x-fastest layout, N3 in the natural one
   const long long inner = ax == 0 ? (c->g.xfast ? (long long)c->n[2] * c->n[0] : (long long)c->n[2])
                                   : (long long)c->n[1] * c->n[2];
-  const long long nrf = fr.nrf < 0 ? (long long)c->krep * c->ns : fr.nrf;
-  const long long outer = ax == 0 ? nrf * (c->g.xfast ? 1 : c->n[0]) : nrf;
-  const long long outer_per_rep = (ax == 0 ? (long long)c->ns * (c->g.xfast ? 1 : c->n[0]) : (long long)c->ns);
+  const long long outer = ax == 0 ? (long long)c->krep * c->ns * (c->g.xfast ? 1 : c->n[0])
+                                  : (long long)c->krep * c->ns;
+  const long long outer_per_rep = outer / c->krep;
   const long long blocks = outer * c->g.tiles[gi];
-  const size_t off = (size_t)fr.rf0 * c->N * vsize_of(c->prec);
   t_begin(c);
   cudaError_t e = launch_strided(prec_code(c->prec), sign, ilog2(L), (unsigned)blocks, c->g.threads[gi], c->g.smem[gi],
-                                 st ? st : c->st, static_cast<char *>(c->S) + off, c->g.lgTI[gi], inner,
-                                 c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0], c->active + fr.rf0 / c->ns, outer_per_rep,
-                                 c->g.pitch[gi], ax == 0 && c->yRev, c->g.nv[gi]);
+                                 c->st, c->S, c->g.lgTI[gi], inner, c->g.tiles[gi], c->tw[ax == 0 ? 1 : 0],
+                                 c->active, outer_per_rep, c->g.pitch[gi], ax == 0 && c->yRev, c->g.nv[gi]);
   t_end(c, ax == 0 ? (sign < 0 ? K_FFT_Y_FWD : K_FFT_Y_INV) : (sign < 0 ? K_FFT_X_FWD : K_FFT_X_INV));
   return e;
 }
@@ -1176,12 +1090,12 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
            "\"b_tiles\": %lld, \"b_mirrored\": %d}, "
            "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
            "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
-           "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"groups\": %d, \"autotune\": ",
+           "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": ",
            1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp,
            g.xTable ? c->ntiles : 0LL, (int)(g.xTable && c->xtSym), 1 << g.lgTI[0], g.threads[0], g.smem[0],
            g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
            radix_plan(c->n[1], g.nv[0] ? g.nv[0] : fft_nv(ilog2(c->n[1]))).c_str(),
-           radix_plan(c->n[2], g.zNV ? g.zNV : zpass_nv(ilog2(c->n[2]), vs)).c_str(), kGraphSteps, step_groups(c));
+           radix_plan(c->n[2], g.zNV ? g.zNV : zpass_nv(ilog2(c->n[2]), vs)).c_str(), kGraphSteps);
   return std::string(b) + tuning + "}";
 }
 
@@ -1189,7 +1103,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
 // times each shape once; later contexts of the shape (serving classes, batch
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
-  int zTL, xLgT, yLgTI, zNV, yNV, zGroups;
+  int zTL, xLgT, yLgTI, zNV, yNV;
   bool xWide, xWarp;
   std::string timings;
 };
@@ -1223,11 +1137,10 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,n=<8|16>,x=<tile columns>,w=<0|1>,y=<tile columns>,m=<8|16>,f=<0|1>,g=<groups>"
+  // PFDD_PLAN="z=<lines>,n=<8|16>,x=<tile columns>,w=<0|1>,y=<tile columns>,m=<8|16>,f=<0|1>"
   // pins the plan (each entry optional, ignored when it does not fit; n and m:
   // values a thread of the z-pass and the y passes, the radix plans; w=1, the
-  // warp-team x-pass, after x; f=0, the y passes in ascending field order;
-  // g: slip-system groups of a step)
+  // warp-team x-pass, after x; f=0, the y passes in ascending field order)
   // instead of timing it, e.g. to profile the plan a timed run chose (a
   // profiler distorts the timings)
   if (const char *pin = std::getenv("PFDD_PLAN")) {
@@ -1237,7 +1150,6 @@ static pfdd_status autotune(pfdd_ctx *c) {
       int v = 0;
       const bool kv = std::sscanf(q, "%c=%d", &key, &v) == 2;
       if (kv && key == 'f') c->yRev = v != 0;
-      if (kv && key == 'g') c->zgroups = std::max(1, std::min(kMaxGroups, v));
       if (kv && v > 0) {
         Geometry g = c->g;
         const long long tt = uses_tile_table(c->prec) ? c->ntiles : 0;
@@ -1278,7 +1190,6 @@ static pfdd_status autotune(pfdd_ctx *c) {
              set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs,
                                   it->second.yNV))) {
           c->g = g;
-          c->zgroups = it->second.zGroups;
           c->gen++;
           c->plan = "{\"cached\": true, \"timings\": " + it->second.timings + "}";
           return PFDD_OK;
@@ -1372,53 +1283,6 @@ static pfdd_status autotune(pfdd_ctx *c) {
       }
       c->g = best;
     }
-    // slip-system groups: whole steps (the stress table zero for the steps
-    // timed), in CUDA graphs when the context uses them, one group first
-    std::string gs;
-    {
-      const int units = c->ns;  // the timings run replica 0 alone
-      const int nst = std::min(4, c->kchunk);
-      int bestG = 1;
-      double bg = 1e30;
-      if (units > 1 && c->N % 32 == 0) {
-        CK(c, cudaMemsetAsync(c->tau, 0, (size_t)nst * c->nrep * c->ns * sizeof(double), c->st));
-        ZParams zp = make_zparams(c);
-        CK(c, ctx_zpass(c, zp, Z_SRC_XI | Z_FWD | Z_STORE));
-        const int cands[] = {1, 2, 3, 4, 6, 12};
-        for (int G : cands) {
-          if (G > units) break;
-          c->zgroups = G;
-          cudaGraphExec_t ge = nullptr;
-          auto steps = [&]() -> cudaError_t {
-            cudaError_t e = cudaMemsetAsync(c->step_ctr, 0xff, sizeof(int), c->st);
-            if (e != cudaSuccess) return e;
-            if (ge) return cudaGraphLaunch(ge, c->st);
-            e = seq_begin(c);
-            for (int s = 0; s < nst && e == cudaSuccess; ++s) e = launch_step<T>(c, zp);
-            if (e == cudaSuccess) e = seq_end(c);
-            return e;
-          };
-          double us = -1.0;
-          if (steps() == cudaSuccess && cudaStreamSynchronize(c->st) == cudaSuccess) {  // direct: smem opt-ins
-            if (c->use_graphs && capture_steps<T>(c, zp, nst, &ge) != cudaSuccess) {
-              cudaGetLastError();
-              ge = nullptr;
-            }
-            us = time_us(steps);
-            if (us > 0) us /= nst;
-          } else {
-            cudaGetLastError();
-          }
-          if (ge) cudaGraphExecDestroy(ge);
-          if (us > 0 && us < bg) { bg = us; bestG = G; }
-          char b[64];
-          snprintf(b, sizeof b, "%s\"%d\": %.1f", gs.empty() ? "" : ", ", G, us);
-          gs += b;
-        }
-      }
-      c->zgroups = bestG;
-      CK(c, cudaStreamSynchronize(c->st));
-    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->launches = l0;
@@ -1431,10 +1295,10 @@ static pfdd_status autotune(pfdd_ctx *c) {
     c->specValid = false;
     c->gen++;  // captured launch shapes change
     tuning = "{\"z_pass_us_by_lines\": {" + zs + "}, \"x_pass_us_by_tile\": {" + xs + "}, \"y_pass_us_by_tile\": {" +
-             ys + "}, \"step_us_by_groups\": {" + gs + "}}";
+             ys + "}}";
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.zNV, c->g.nv[0], c->zgroups,
+      g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.zNV, c->g.nv[0],
                                c->g.xWide, c->g.xWarp, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
@@ -1505,90 +1369,23 @@ static void diag_energies(const pfdd_ctx *c, const double *g, double *out) {
 }
 
 // The launches of one TDGL step (step index taken from the device counter).
-// Slip-system groups a step runs with: the plan's count, capped by the units
-// (systems of replica 0 when krep == 1, else replicas); one group in kernel
-// timing mode (per-kernel events on the context's stream), with diagnostics
-// (a gather after the whole z-pass), and for grids whose field size is not a
-// whole number of 32-bit words of the pinned-point bit mask.
-static int step_groups(const pfdd_ctx *c) {
-  if (c->zgroups <= 1 || c->tm.on || c->diagOn || !c->g.xfast || c->N % 32 != 0) return 1;
-  return std::min(c->zgroups, c->krep == 1 ? c->ns : c->krep);
-}
-
-static FieldRange group_range(const pfdd_ctx *c, int g, int G) {
-  const int units = c->krep == 1 ? c->ns : c->krep, per = c->krep == 1 ? 1 : c->ns;
-  const int u0 = (int)((long long)g * units / G), u1 = (int)((long long)(g + 1) * units / G);
-  return FieldRange{u0 * per, (u1 - u0) * per};
-}
-
-// A sequence of grouped steps forks yst and zst off the context's stream
-// (after everything queued on it) and joins them back at its end.
-static cudaError_t seq_begin(pfdd_ctx *c) {
-  if (step_groups(c) <= 1) return cudaSuccess;
-  cudaError_t e = ensure_aux_streams(c);
-  if (e == cudaSuccess) e = cudaEventRecord(c->ev_fork, c->st);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->yst, c->ev_fork, 0);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->zst, c->ev_fork, 0);
-  c->seq_fresh = true;
-  return e;
-}
-
-static cudaError_t seq_end(pfdd_ctx *c) {
-  if (step_groups(c) <= 1) return cudaSuccess;
-  cudaError_t e = cudaEventRecord(c->ev_yend, c->yst);
-  if (e == cudaSuccess) e = cudaEventRecord(c->ev_zend, c->zst);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->st, c->ev_yend, 0);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->st, c->ev_zend, 0);
-  return e;
-}
-
 template <typename T>
 static cudaError_t launch_step(pfdd_ctx *c, ZParams &zp) {
-  const int G = step_groups(c);
-  if (G <= 1) {
-    cudaError_t e = ctx_strided(c, -1, 0);
-    if (e == cudaSuccess) e = launch_x_fused<T>(c);
-    if (e == cudaSuccess) e = ctx_strided(c, +1, 0);
-    if (e == cudaSuccess) e = ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE);
-    if (e == cudaSuccess && c->diagOn) e = launch_diag_gather(c, c->step_ctr);
-    return e;
-  }
-  // Grouped: group g's y-forward follows its own z-pass of the previous step
-  // (stream yst), the x-pass on st waits for every group's, then yst runs the
-  // y-inverse group by group and zst each group's z-pass as soon as its
-  // y-inverse is done.  So the y-inverse of group g + 1 and the y-forward of
-  // group g - 1 run beside the z-pass of group g.
-  cudaError_t e = cudaSuccess;
-  for (int g = 0; g < G && e == cudaSuccess; ++g) {
-    if (!c->seq_fresh) e = cudaStreamWaitEvent(c->yst, c->ev_z[g], 0);
-    if (e == cudaSuccess) e = ctx_strided(c, -1, 0, group_range(c, g, G), c->yst);
-  }
-  c->seq_fresh = false;
-  if (e == cudaSuccess) e = cudaEventRecord(c->ev_y, c->yst);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->st, c->ev_y, 0);
+  cudaError_t e = ctx_strided(c, -1, 0);
   if (e == cudaSuccess) e = launch_x_fused<T>(c);
-  if (e == cudaSuccess) e = cudaEventRecord(c->ev_x, c->st);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->yst, c->ev_x, 0);
-  for (int g = 0; g < G && e == cudaSuccess; ++g) {
-    const FieldRange fr = group_range(c, g, G);
-    e = ctx_strided(c, +1, 0, fr, c->yst);
-    if (e == cudaSuccess) e = cudaEventRecord(c->ev_yi[g], c->yst);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->zst, c->ev_yi[g], 0);
-    if (e == cudaSuccess) e = ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE, fr, c->zst);
-    if (e == cudaSuccess) e = cudaEventRecord(c->ev_z[g], c->zst);
-  }
+  if (e == cudaSuccess) e = ctx_strided(c, +1, 0);
+  if (e == cudaSuccess) e = ctx_zpass(c, zp, Z_INV | Z_UPDATE | Z_FWD | Z_STORE);
+  if (e == cudaSuccess && c->diagOn) e = launch_diag_gather(c, c->step_ctr);
   return e;
 }
 
 // Captures `steps` steps on the context's stream into an executable graph.
 template <typename T>
 static cudaError_t capture_steps(pfdd_ctx *c, ZParams &zp, int steps, cudaGraphExec_t *out) {
-  cudaError_t e = ensure_aux_streams(c);  // (made outside the capture)
-  if (e == cudaSuccess) e = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal);
+  cudaError_t e = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  cudaError_t le = seq_begin(c);
+  cudaError_t le = cudaSuccess;
   for (int s = 0; s < steps && le == cudaSuccess; ++s) le = launch_step<T>(c, zp);
-  if (le == cudaSuccess) le = seq_end(c);
   cudaGraph_t g = nullptr;
   e = cudaStreamEndCapture(c->st, &g);
   if (le != cudaSuccess) e = le;
@@ -1627,9 +1424,7 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
       // direct launches: timing mode, and the first step of a context (it
       // also sets every kernel's shared-memory opt-in before any capture)
       const int n = direct ? ks : 1;
-      CK(c, seq_begin(c));
       for (; done < n; ++done) CK(c, launch_step<T>(c, zp));
-      CK(c, seq_end(c));
       c->primed = true;
     }
     if (done < ks) {
@@ -1638,13 +1433,12 @@ static pfdd_status run_steps(pfdd_ctx *c, int nsteps, const double *tau, double 
         if (c->graph_one) cudaGraphExecDestroy(c->graph_one);
         c->graph_many = c->graph_one = nullptr;
         const long long l0 = c->launches;
-        CK(c, capture_steps<T>(c, zp, 1, &c->graph_one));
-        c->graph_launches = c->launches - l0;  // kernels a step
         CK(c, capture_steps<T>(c, zp, kGraphSteps, &c->graph_many));
+        CK(c, capture_steps<T>(c, zp, 1, &c->graph_one));
         c->launches = l0;  // captured, not launched
         c->graph_gen = c->gen;
       }
-      const long long per_step = c->graph_launches;
+      const int per_step = 4 + (c->diagOn ? 1 : 0);
       for (; done + kGraphSteps <= ks; done += kGraphSteps) {
         CK(c, cudaGraphLaunch(c->graph_many, c->st));
         c->launches += (long long)per_step * kGraphSteps;
@@ -1906,7 +1700,6 @@ extern "C" pfdd_status pfdd_set_stream_priority(pfdd_ctx *c, int priority) {
   }
   cudaStreamDestroy(c->st);
   c->st = ns;
-  destroy_aux_streams(c);  // remade with the new priority on next use
   return PFDD_OK;
 }
 

@@ -53,9 +53,6 @@ def test_tuned_plan_gives_same_bits(native_lib, precision):
     assert p0["radix_plan"] == ["8x4", "16", "8x8"]  # 16 values a thread for the 16-long y lines
     assert p1["radix_plan"][1] in ("16", "8x2") and p1["radix_plan"][2] in ("8x8", "16x4")
     assert any("/16" in k for k in tune["z_pass_us_by_lines"]) and any("/8" in k for k in tune["z_pass_us_by_lines"])
-    groups = tune["step_us_by_groups"]  # whole steps by slip-system groups, one group first
-    assert list(groups)[:4] == ["1", "2", "3", "4"] and all(v > 0 for v in groups.values())
-    assert str(p1["groups"]) in groups and p0["groups"] == 1
 
 
 def test_pinned_plan(native_lib):
@@ -203,35 +200,3 @@ def test_every_radix_plan_matches_oracle(native_lib, precision):
             assert np.max(np.abs(g[:, 0] - go) / np.abs(go)) <= gtol, (zn, yn)
             seen.add(x.tobytes())
     assert len(seen) >= 2  # the plans really differ in rounding
-
-
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("groups", [2, 5, 12])
-def test_slip_system_groups_same_bits(native_lib, precision, groups):
-    """Steps run in slip-system groups (each group's y passes and z-pass on two
-    more streams, beside the other groups' work) give the bits of one-group
-    steps: a solve with pinned points and per-system coefficients, a solve
-    under a stress field, and a batch of three (groups of whole replicas).
-    20 steps: the first direct, then a 16-step graph and 1-step graphs."""
-    n = (32, 16, 16)
-    spec = workloads.SolveSpec(n=n, ns=12, steps=20, sigma_max=0.05, noise_seed=40,
-                               loops=workloads.random_loops(n, 3, 1.0, 4.0, 12, seed=40))
-    rng = np.random.default_rng(40)
-    x0, b0 = workloads.initial_state(spec)
-    bc = (rng.random(b0.shape) < 0.1).astype(np.float64)
-    cd2 = np.linspace(0.005, 0.02, 12)
-
-    def pins(s, _):
-        s.set_params(cd2, np.linspace(0.05, 0.15, 12), 1.0)
-        s.set_state(x0, bc)
-
-    def field(s, _):
-        s.set_tau_field(rng_tf)
-
-    rng_tf = np.random.default_rng(41).uniform(-0.1, 0.1, size=(spec.npts, 12))
-    for prep, nrep in ((pins, 1), (field, 1), (None, 3)):
-        g1, x1, p1 = pinned(spec, precision, "g=1", nrep=nrep, prepare=prep)
-        gg, xg, pg = pinned(spec, precision, f"g={groups}", nrep=nrep, prepare=prep)
-        assert p1["groups"] == 1 and pg["groups"] == min(groups, 12 if nrep == 1 else nrep)
-        np.testing.assert_array_equal(g1, gg)
-        np.testing.assert_array_equal(x1, xg)
