@@ -134,7 +134,8 @@ pfdd_status pfdd_step(pfdd_ctx *ctx, int nsteps, const double *tau, double *gamm
  * passing step whose window is not full resets the count, and the loop ends
  * at the fifth count.  tau[max_steps][ns] as for pfdd_step; gamma[max_steps]
  * and gamma_a[max_steps][ns] (may be NULL) receive the steps that ran;
- * *steps_done = how many (== max_steps when the loop did not converge).  The
+ * *steps_done = how many (== max_steps when the loop did not converge; on an
+ * error, the steps of the chunks completed before it).  The
  * pass marks carry over between calls, so a loop may be run in pieces.  The
  * state after the call is the state after the last step that ran: steps run
  * in chunks, and a chunk that ran past the stop is rewound (a device copy of

@@ -1569,7 +1569,10 @@ extern "C" pfdd_status pfdd_step_converge(pfdd_ctx *c, int max_steps, const doub
     CK(c, cudaMemcpyAsync(c->xi_snap, c->xi, xbytes, cudaMemcpyDeviceToDevice, c->st));
     double *ga = gamma_a ? gamma_a + (size_t)done * ns : nullptr;
     pfdd_status st = pfdd_step(c, k, tau + (size_t)done * ns, gamma + done, ga);
-    if (st != PFDD_OK) return st;
+    if (st != PFDD_OK) {
+      *steps_done = done;  // the chunks before this one
+      return st;
+    }
     int stop = -1;
     for (int j = 0; j < k && stop < 0; ++j)
       if (converge_update(c, gamma[done + j])) stop = j;
@@ -1581,7 +1584,10 @@ extern "C" pfdd_status pfdd_step_converge(pfdd_ctx *c, int max_steps, const doub
       CK(c, cudaMemcpyAsync(c->xi, c->xi_snap, xbytes, cudaMemcpyDeviceToDevice, c->st));
       c->specValid = false;
       st = pfdd_step(c, stop + 1, tau + (size_t)done * ns, gamma + done, ga);
-      if (st != PFDD_OK) return st;
+      if (st != PFDD_OK) {
+        *steps_done = done;
+        return st;
+      }
     }
     done += stop + 1;
     break;
