@@ -129,10 +129,10 @@ pfdd_status pfdd_step(pfdd_ctx *ctx, int nsteps, const double *tau, double *gamm
  * pfdd_step_converge then runs up to max_steps steps like pfdd_step and stops
  * after the step at which the reference leaves the loop: a step passes when
  * |(gamma - gamma_last) / gamma| < 1e-8 or |gamma| < 1e-12 (for gamma == 0:
- * |gamma - gamma_last| < 1e-15 or |gamma| < 1e-14); once 30 steps in a row
- * have passed, each further passing step with a full window counts, a
- * passing step whose window is not full resets the count, and the loop ends
- * at the fifth count.  tau[max_steps][ns] as for pfdd_step; gamma[max_steps]
+ * |gamma - gamma_last| < 1e-15 or |gamma| < 1e-14); from the loop's 30th
+ * step on, a passing step adds one to a count when it and the 29 steps before
+ * it all passed and resets the count otherwise (a failing step leaves it),
+ * and the loop ends at the fifth count.  tau[max_steps][ns] as for pfdd_step; gamma[max_steps]
  * and gamma_a[max_steps][ns] (may be NULL) receive the steps that ran;
  * *steps_done = how many (== max_steps when the loop did not converge; on an
  * error, the steps of the chunks completed before it).  The
