@@ -1562,7 +1562,6 @@ extern "C" pfdd_status pfdd_step_converge(pfdd_ctx *c, int max_steps, const doub
   const size_t xbytes = (size_t)c->ns * c->N * sizeof(double2);
   if (!c->xi_snap) CK(c, cudaMalloc(&c->xi_snap, xbytes));
   const int ns = c->ns;
-  std::vector<double> ga_tmp;
   int done = 0;
   while (done < max_steps) {
     const int k = std::min(c->kchunk, max_steps - done);
