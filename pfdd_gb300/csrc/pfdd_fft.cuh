@@ -196,7 +196,7 @@ __device__ __forceinline__ void line_fft(int th, int lgL_rt, const V *tw, Addr s
   constexpr int lgNV = NV == 16 ? 4 : 3;
   const int lgL = LG >= 0 ? LG : lgL_rt;
   if (lgL >= 3) {
-    const int LV = 1 << (lgL - lgNV);
+    const int LV = 1 << (lgL > lgNV ? lgL - lgNV : 0);  // (L >= NV whenever this runs)
     // stage count (run time: at most 4 for L <= 4096)
     constexpr int NST = LG >= 0 ? stockham_stages(LG, NV) : stockham_stages(12, NV);
 #pragma unroll

@@ -207,9 +207,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) zpass_kernel(ZPar
   const int bf = lf0 / TL;
   const int x0 = xf ? (bf % xblocks) * TL : 0, yj = xf ? bf / xblocks : 0;
   // field-relative offsets (< 2^31): xi element (line t, z = k) at lb + t*ls + k,
-  // S element at sb + t*st + k*sk
+  // S element at sb + t + k*sk (x-fastest layout; sb + t*L + k in the natural one)
   const int lb = xf ? (x0 * p.n2 + yj) * L : lf0 * L, ls = xf ? p.n2 * L : L;
-  const int sb = xf ? yj * L * p.n1 + x0 : lf0 * L, st = xf ? 1 : L, sk = xf ? p.n1 : 1;
+  const int sb = xf ? yj * L * p.n1 + x0 : lf0 * L, sk = xf ? p.n1 : 1;
   const long long fbase = rf * p.N;  // element / bit base of this field
   const int nel = TL << lgL;
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -378,23 +378,23 @@ fft_strided_kernel(void *data_, int lgL, int lgTI, long long inner, long long ti
     for (int m = 0; m < NV; ++m) v[m] = col[(th + m * LV) * in32];
     line_fft_io<S, LG, true, true, NV>(v, th, tws, [&](int l) { return &sm[l * pitch + t]; },
                                        [&](int l) { return &col[l * in32]; }, true);
-    return;
-  }
-  for (int e = tid; e < nel; e += nthr) {
-    const int l = e >> lgTI, t = e & (TI - 1);
-    cp_async_elem(&sm[l * pitch + t], &base[(long long)l * inner + t]);
-  }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  const int E = L >= 8 ? 8 : L, team = L / E;  // LG < 3 here: one thread per line
-  const int t = tid & (TI - 1), th = tid >> lgTI;  // consecutive lanes on consecutive lines
-  const bool act = th < team;
-  line_fft<S, LG>(th, lgL, tws, [&](int l) { return &sm[l * pitch + t]; }, act);
-  __syncthreads();
-  for (int e = tid; e < nel; e += nthr) {
-    const int l = e >> lgTI, tt = e & (TI - 1);
-    base[(long long)l * inner + tt] = sm[l * pitch + tt];
+  } else {
+    for (int e = tid; e < nel; e += nthr) {
+      const int l = e >> lgTI, t = e & (TI - 1);
+      cp_async_elem(&sm[l * pitch + t], &base[(long long)l * inner + t]);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    const int E = L >= 8 ? 8 : L, team = L / E;  // LG < 3 here: one thread per line
+    const int t = tid & (TI - 1), th = tid >> lgTI;  // consecutive lanes on consecutive lines
+    const bool act = th < team;
+    line_fft<S, LG>(th, lgL, tws, [&](int l) { return &sm[l * pitch + t]; }, act);
+    __syncthreads();
+    for (int e = tid; e < nel; e += nthr) {
+      const int l = e >> lgTI, tt = e & (TI - 1);
+      base[(long long)l * inner + tt] = sm[l * pitch + tt];
+    }
   }
 }
 
