@@ -1040,6 +1040,7 @@ static cudaError_t launch_x_fused(pfdd_ctx *c) {
   xp.bf = c->bf;
   xp.err = c->errflag;
   xp.drop_bulk = c->drop_bulk;
+  xp.bsplit = c->g.xSplit ? c->ns * (c->ns + 1) / 4 : 0;  // P / 2 pair rows first
   xp.wait_ns = c->drop_bulk ? kTestWaitNs : kWaitNs;
   cudaError_t e = c->g.xWarp
                       ? launch_x_warp_f32(c->ns, c->prec == PFDD_FFT_FP32_BFLY, blocks, c->g.xThreads, c->g.xSmem, c->st, xp)
@@ -1087,12 +1088,12 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
   snprintf(b, sizeof b,
            "{\"x_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"ctas\": %lld, \"warp_teams\": %d, "
 
-           "\"b_tiles\": %lld, \"b_mirrored\": %d}, "
+           "\"b_tiles\": %lld, \"b_mirrored\": %d, \"b_split\": %d}, "
            "\"y_pass\": {\"tile_columns\": %d, \"threads\": %d, \"smem\": %zu, \"tiles_per_field\": %lld}, "
            "\"z_pass\": {\"lines\": %d, \"threads\": %d, \"smem\": %zu}, "
            "\"radix_plan\": [\"%s\", \"%s\", \"%s\"], \"graph_steps\": %d, \"autotune\": ",
            1 << g.xLgT, g.xThreads, g.xSmem, (long long)c->nrep * g.xTiles, (int)g.xWarp,
-           g.xTable ? c->ntiles : 0LL, (int)(g.xTable && c->xtSym), 1 << g.lgTI[0], g.threads[0], g.smem[0],
+           g.xTable ? c->ntiles : 0LL, (int)(g.xTable && c->xtSym), (int)g.xSplit, 1 << g.lgTI[0], g.threads[0], g.smem[0],
            g.tiles[0], g.zTL, g.zThreads, g.zSmem, radix_plan(c->n[0], xnv).c_str(),
            radix_plan(c->n[1], g.nv[0] ? g.nv[0] : fft_nv(ilog2(c->n[1]))).c_str(),
            radix_plan(c->n[2], g.zNV ? g.zNV : zpass_nv(ilog2(c->n[2]), vs)).c_str(), kGraphSteps);
@@ -1104,7 +1105,7 @@ static std::string plan_json(const pfdd_ctx *c, const std::string &tuning) {
 // re-creation) reuse the plan instead of timing under whatever else is running.
 struct TunedPlan {
   int zTL, xLgT, yLgTI, zNV, yNV;
-  bool xWide, xWarp;
+  bool xWide, xWarp, xSplit;
   std::string timings;
 };
 static std::mutex g_plan_mu;
@@ -1137,10 +1138,11 @@ template <typename T>
 static pfdd_status autotune(pfdd_ctx *c) {
   c->tuned = true;
   std::string tuning = "null";
-  // PFDD_PLAN="z=<lines>,n=<8|16>,x=<tile columns>,w=<0|1>,y=<tile columns>,m=<8|16>,f=<0|1>"
+  // PFDD_PLAN="z=<lines>,n=<8|16>,x=<tile columns>,w=<0|1|2>,y=<tile columns>,m=<8|16>,f=<0|1>"
   // pins the plan (each entry optional, ignored when it does not fit; n and m:
   // values a thread of the z-pass and the y passes, the radix plans; w=1, the
-  // warp-team x-pass, after x; f=0, the y passes in ascending field order)
+  // warp-team x-pass, after x, w=2 the same with its B block in two halves;
+  // f=0, the y passes in ascending field order)
   // instead of timing it, e.g. to profile the plan a timed run chose (a
   // profiler distorts the timings)
   if (const char *pin = std::getenv("PFDD_PLAN")) {
@@ -1160,7 +1162,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
                         : key == 'x' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, ilog2(v), false,
                                                       false, tt)
                         : key == 'w' ? set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, g.xLgT, false,
-                                                      v == 1, tt)
+                                                      v >= 1, tt, v == 2)
                         : key == 'y' ? set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], ilog2(v), vs,
                                                             g.nv[0])
                                      : false;
@@ -1185,7 +1187,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
         if (set_z_geometry(g, c->n[0], c->n[1], c->n[2], vs, it->second.zTL, it->second.zNV) &&
             g.zNparts <= c->zparts_cap &&
             set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, it->second.xLgT, it->second.xWide,
-                           it->second.xWarp, uses_tile_table(c->prec) ? c->ntiles : 0) &&
+                           it->second.xWarp, uses_tile_table(c->prec) ? c->ntiles : 0, it->second.xSplit) &&
             (c->n[1] == 1 ||
              set_strided_geometry(g, 0, c->n[1], (long long)c->n[2] * c->n[0], it->second.yLgTI, vs,
                                   it->second.yNV))) {
@@ -1251,20 +1253,21 @@ static pfdd_status autotune(pfdd_ctx *c) {
     c->g = best;
     bt = 1e30;
     // tile widths 1..64, each with the block-team kernel (plain and wide) and
-    // the warp-team kernel (key suffix "v"); all compute the same bits
-    for (int cand = 0; cand <= 3 * 7 - 1; ++cand) {
-      const int lgT = cand / 3, form = cand % 3;
-      const bool wide = form == 1, warp = form == 2;
+    // the warp-team kernel (key suffix "v"; "s": its B block in two halves, for
+    // a fourth CTA on an SM); all compute the same bits
+    for (int cand = 0; cand <= 4 * 7 - 1; ++cand) {
+      const int lgT = cand / 4, form = cand % 4;
+      const bool wide = form == 1, warp = form >= 2, split = form == 3;
       Geometry g = c->g;
       if (!set_x_geometry(g, c->n[0], c->n[1], c->n[2], c->ns, vs, bs, lgT, wide, warp,
-                          uses_tile_table(c->prec) ? c->ntiles : 0))
+                          uses_tile_table(c->prec) ? c->ntiles : 0, split))
         continue;
       c->g = g;
       const double us = time_us([&] { return launch_x_fused<T>(c); });
       if (us > 0 && us < bt) { bt = us; best = g; }
       char b[64];
       snprintf(b, sizeof b, "%s\"%d%s\": %.1f", xs.empty() ? "" : ", ", 1 << lgT,
-               wide ? "w" : (warp ? "v" : ""), us);
+               wide ? "w" : (split ? "s" : (warp ? "v" : "")), us);
       xs += b;
     }
     c->g = best;
@@ -1299,7 +1302,7 @@ static pfdd_status autotune(pfdd_ctx *c) {
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
       g_plans[key] = TunedPlan{c->g.zTL, c->g.xLgT, c->g.lgTI[0], c->g.zNV, c->g.nv[0],
-                               c->g.xWide, c->g.xWarp, tuning};
+                               c->g.xWide, c->g.xWarp, c->g.xSplit, tuning};
     }
     cudaMemsetAsync(c->errflag, 0, sizeof(int), c->st);
   }

@@ -473,6 +473,9 @@ struct XParams {
   // nothing is left in flight
   int drop_bulk;
   unsigned long long wait_ns;
+  // > 0 (warp teams on the tile table): the B block's first bsplit pair rows
+  // arrive first; the rest reuse the same buffer once those have been used
+  int bsplit;
   BFlyParams bf;
 };
 
@@ -520,6 +523,43 @@ __device__ __forceinline__ void contract_table(const T *Bs, int Wrt, int bx, At 
   }
 #pragma unroll
   for (int a = 0; a < NS; ++a) at(a) = out[a];
+}
+
+// contract_table (FP32, inputs in registers, row width WC) with the tile's pair
+// rows in two halves through one buffer: rows [0, P/2) are in Bs on entry;
+// at pair P/2 every thread calls mid(), which refills Bs with rows [P/2, P).
+// The additions are those of contract_table in the same order (the same
+// bits).  has: this thread has a point (a thread without one still calls
+// mid(), which holds block barriers).
+template <int NS, int WC, typename At, typename Mid>
+__device__ __forceinline__ void contract_table_split(const float *Bs, int bx, bool has, At at, Mid mid) {
+  constexpr int P = NS * (NS + 1) / 2, P0 = P / 2;
+  Bs += bx;
+  float2 out[NS], in[NS];
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+    out[a] = make_float2(0.f, 0.f);
+    in[a] = has ? at(a) : make_float2(0.f, 0.f);
+  }
+  int pidx = 0;
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+#pragma unroll
+    for (int b = a; b < NS; ++b, ++pidx) {
+      if (pidx == P0) mid();
+      const float v = Bs[(pidx < P0 ? pidx : pidx - P0) * WC];
+      out[a].x += in[b].x * v;
+      out[a].y += in[b].y * v;
+      if (b != a) {
+        out[b].x += in[a].x * v;
+        out[b].y += in[a].y * v;
+      }
+    }
+  }
+  if (has) {
+#pragma unroll
+    for (int a = 0; a < NS; ++a) at(a) = out[a];
+  }
 }
 
 // The same contraction with the closed form of Bmatrix (F:328-412) in FP32:
@@ -750,11 +790,13 @@ __host__ __device__ __forceinline__ int xw_swz(int l, int lgL) {
 }
 
 // Shared-memory bytes of the warp-team x-pass: twiddles | tile lines |
-// B tile (bsize 0: B evaluated in registers).
-__host__ __device__ __forceinline__ size_t xw_smem(int ns, int lgL, int lgT, size_t bsize, bool table = false) {
+// B tile (bsize 0: B evaluated in registers; split: the larger half of its
+// pair rows, P - P/2).
+__host__ __device__ __forceinline__ size_t xw_smem(int ns, int lgL, int lgT, size_t bsize, bool table = false,
+                                                   bool split = false) {
   const size_t head = (((size_t)1 << lgL) + (size_t)ns * ((size_t)1 << lgT) * xw_pitch(lgL)) * 8;
-  const size_t P = (size_t)ns * (ns + 1) / 2;
-  return ((head + 15) & ~(size_t)15) + P * (table ? ((size_t)1 << lgL) + 4 : (size_t)1 << (lgL + lgT)) * bsize;
+  const size_t P = (size_t)ns * (ns + 1) / 2, rows = split ? P - P / 2 : P;
+  return ((head + 15) & ~(size_t)15) + rows * (table ? ((size_t)1 << lgL) + 4 : (size_t)1 << (lgL + lgT)) * bsize;
 }
 
 // Fused x-pass with warp-resident line teams (FP32 spectra, N1 = 32..256):
@@ -817,8 +859,10 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
   if (!idle) {
     if (!BFLY && tid == 0) {  // B tile: bvals contiguous values (a multiple of 16 bytes)
       mbar_init(&bbar, 1);
-      if (p.drop_bulk && blockIdx.x == 0) mbar_arrive_expect_tx(&bbar, (unsigned)(bvals * 4));
-      else bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(bvals * 4), &bbar);
+      // split: the first p.bsplit pair rows now, the rest during the contraction
+      const int first = p.bsplit ? p.bsplit * W : bvals;
+      if (p.drop_bulk && blockIdx.x == 0) mbar_arrive_expect_tx(&bbar, (unsigned)(first * 4));
+      else bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + boff, (unsigned)(first * 4), &bbar);
     }
     load_twiddles(tws, reinterpret_cast<const V *>(p.tw), L);
   }
@@ -839,32 +883,68 @@ __global__ void __launch_bounds__(384, 2) x_warp_kernel(XParams p) {
     line_fft_io<-1, LG, true, false, NV, true>(v, th, tws, [&](int l) { return &line[xw_swz(l, LG)]; },
                                                [&](int l) { return &line[xw_swz(l, LG)]; }, act);
   }
-  if (!BFLY) mbar_wait(&bbar, 0, p.err, p.wait_ns);
+  bool bok = true;
+  if (!BFLY) bok = mbar_wait(&bbar, 0, p.err, p.wait_ns);
   __syncthreads();
-  for (int q = tid; q < (tl << LG); q += nthr) {
-    const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
-    V *const pt = sm + t * LP + sx;  // the point's value of field a at pt[a * T * LP]
-    if constexpr (BFLY) {
-      contract_bfly<NS>(p.bf, [&](int a) -> V & { return pt[a * TT * LP]; }, x, L, c0 + t);
-    } else {
-      const int role = lgT == 0 ? role0 : t;
-      const int bx = !tabled ? q : (role == 0 ? x : (x == L / 2 ? L : b_mirror(x, L)));
-      // the table form's row widths (a mirrored pair, a single line) and tile
-      // widths (T = 1, 2) as constants: every shared-memory access of the
-      // contraction is an immediate offset from pt or from the B row
-      auto table = [&](auto wc, auto tc) {
-        constexpr int WC = decltype(wc)::value, TC = decltype(tc)::value;
-        contract_table<float, NS, true, WC>(Bs, W, bx, [&](int a) -> V & { return pt[a * TC * LP]; });
-      };
-      using I = std::integral_constant<int, 1>;
-      using II = std::integral_constant<int, 2>;
-      using WM = std::integral_constant<int, b_wm(L)>;
-      using WS = std::integral_constant<int, L>;
-      if (tabled && mirrored && lgT == 1) table(WM{}, II{});
-      else if (tabled && mirrored && lgT == 0) table(WM{}, I{});
-      else if (tabled && W == L && lgT == 1) table(WS{}, II{});
-      else if (tabled && W == L && lgT == 0) table(WS{}, I{});
-      else contract_table<float, NS, true>(Bs, W, bx, [&](int a) -> V & { return pt[a * TT * LP]; });
+  if (!BFLY && p.bsplit) {
+    // B block in two halves (the host checks that the tile has at most one
+    // point a thread): every thread takes part in the buffer swap
+    const int q = tid;
+    const bool has = q < (tl << LG);
+    const int t = has ? q >> LG : 0, x = has ? q & (L - 1) : 0;
+    V *const pt = sm + t * LP + xw_swz(x, LG);
+    const int role = lgT == 0 ? role0 : t;
+    const int bx = !has ? 0 : (role == 0 ? x : (x == L / 2 ? L : b_mirror(x, L)));
+    auto mid = [&]() {
+      // every thread is past the first rows (and they had arrived): refill the
+      // buffer with the rest (generic-proxy reads before the bulk copy's writes)
+      if (__syncthreads_and(bok)) {
+        if (tid == 0) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          bulk_load_evict_first(Bs, reinterpret_cast<const float *>(p.B) + boff + (long long)p.bsplit * W,
+                                (unsigned)((bvals - p.bsplit * W) * 4), &bbar);
+        }
+        mbar_wait(&bbar, 1, p.err, p.wait_ns);
+      }
+    };
+    auto split = [&](auto wc, auto tc) {
+      constexpr int WC = decltype(wc)::value, TC = decltype(tc)::value;
+      contract_table_split<NS, WC>(Bs, bx, has, [&](int a) -> V & { return pt[a * TC * LP]; }, mid);
+    };
+    using I = std::integral_constant<int, 1>;
+    using II = std::integral_constant<int, 2>;
+    using WM = std::integral_constant<int, b_wm(L)>;
+    using WS = std::integral_constant<int, L>;
+    if (mirrored && lgT == 1) split(WM{}, II{});
+    else if (mirrored) split(WM{}, I{});
+    else if (lgT == 1) split(WS{}, II{});
+    else split(WS{}, I{});
+  } else {
+    for (int q = tid; q < (tl << LG); q += nthr) {
+      const int t = q >> LG, x = q & (L - 1), sx = xw_swz(x, LG);
+      V *const pt = sm + t * LP + sx;  // the point's value of field a at pt[a * T * LP]
+      if constexpr (BFLY) {
+        contract_bfly<NS>(p.bf, [&](int a) -> V & { return pt[a * TT * LP]; }, x, L, c0 + t);
+      } else {
+        const int role = lgT == 0 ? role0 : t;
+        const int bx = !tabled ? q : (role == 0 ? x : (x == L / 2 ? L : b_mirror(x, L)));
+        // the table form's row widths (a mirrored pair, a single line) and tile
+        // widths (T = 1, 2) as constants: every shared-memory access of the
+        // contraction is an immediate offset from pt or from the B row
+        auto table = [&](auto wc, auto tc) {
+          constexpr int WC = decltype(wc)::value, TC = decltype(tc)::value;
+          contract_table<float, NS, true, WC>(Bs, W, bx, [&](int a) -> V & { return pt[a * TC * LP]; });
+        };
+        using I = std::integral_constant<int, 1>;
+        using II = std::integral_constant<int, 2>;
+        using WM = std::integral_constant<int, b_wm(L)>;
+        using WS = std::integral_constant<int, L>;
+        if (tabled && mirrored && lgT == 1) table(WM{}, II{});
+        else if (tabled && mirrored && lgT == 0) table(WM{}, I{});
+        else if (tabled && W == L && lgT == 1) table(WS{}, II{});
+        else if (tabled && W == L && lgT == 0) table(WS{}, I{});
+        else contract_table<float, NS, true>(Bs, W, bx, [&](int a) -> V & { return pt[a * TT * LP]; });
+      }
     }
   }
   __syncthreads();

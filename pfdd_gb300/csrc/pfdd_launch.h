@@ -79,7 +79,9 @@ struct Geometry {
   // fused x-pass; xWarp: the warp-team kernel (x_warp_kernel); xTable: the
   // B(k) tile-table layout (see BLayout), xTiles then the table's tile count
   int xLgT = 0, xPitch = 1, xThreads = 256;
-  bool xWide = false, xWarp = false, xTable = false;
+  // xSplit (warp teams on the tile table): the tile's B block arrives in two
+  // halves of its pair rows through one buffer of half the size
+  bool xWide = false, xWarp = false, xTable = false, xSplit = false;
   long long xTiles = 1;
   size_t xSmem = 0;
 };
@@ -139,18 +141,20 @@ inline bool set_strided_geometry(Geometry &g, int ax, int L, long long inner, in
 // table_tiles > 0: the tile-table layout with that many tiles (T = 2: a CTA
 // per tile, T = 1: a CTA per line).
 inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t vsize, size_t bsize, int lgT,
-                           bool wide = false, bool warp = false, long long table_tiles = 0) {
+                           bool wide = false, bool warp = false, long long table_tiles = 0, bool split = false) {
   const long long innerx = (long long)n2 * n3;
   if ((1LL << lgT) > innerx && table_tiles == 0) return false;
   if (table_tiles > 0 && lgT > 1) return false;
+  if (split && (!warp || table_tiles == 0 || ns < 2)) return false;
   if (warp) {  // FP32 spectra, N1 = 32..256; a thread a point, at most 384
     const int lgL = ilog2(n1);
     if (wide || vsize != 8 || n1 < 32 || n1 > 256) return false;
-    const size_t smem = xw_smem(ns, lgL, lgT, bsize, table_tiles > 0);
+    const size_t smem = xw_smem(ns, lgL, lgT, bsize, table_tiles > 0, split);
     if (smem > kMaxDynSmem) return false;
     const int lpw = 32 / xw_lv(lgL), lines = ns << lgT;
     int thr = std::max(n1 << lgT, (lines + lpw - 1) / lpw * 32);
     thr = std::min(384, (thr + 31) / 32 * 32);
+    if (split && (n1 << lgT) > thr) return false;  // the split contraction takes one point a thread
     g.xPitch = xw_pitch(lgL);
     g.xLgT = lgT;
     g.xTiles = table_tiles > 0 ? (lgT == 1 ? table_tiles : innerx) : innerx >> lgT;
@@ -159,9 +163,11 @@ inline bool set_x_geometry(Geometry &g, int n1, int n2, int n3, int ns, size_t v
     g.xWide = false;
     g.xWarp = true;
     g.xTable = table_tiles > 0;
+    g.xSplit = split;
     return true;
   }
   g.xWarp = false;
+  g.xSplit = false;
   const int pitch = line_pitch(n1);
   const size_t smem = x_fused_smem(ns, n1, lgT, pitch, vsize, bsize, table_tiles > 0);
   if (smem > kMaxDynSmem) return false;

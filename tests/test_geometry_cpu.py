@@ -79,6 +79,17 @@ int main() {
                 CHECK(h.xTable && h.xSmem <= kMaxDynSmem && h.xThreads % 32 == 0 && h.xThreads <= 384, "table x");
                 CHECK(h.xSmem == (warp ? xw_smem(ns, ilog2(n1), lg, bs, true)
                                        : x_fused_smem(ns, n1, lg, h.xPitch, vs, bs, true)), "table x smem");
+                CHECK(!h.xSplit, "split only when asked");
+                // the warp-team kernel with its B block in two halves: half the pair
+                // rows (rounded up) in shared memory, at most one point a thread
+                Geometry hs = t;
+                if (warp && set_x_geometry(hs, n1, n2, n3, ns, vs, bs, lg, false, true, tiles, true)) {
+                  const size_t P = (size_t)ns * (ns + 1) / 2;
+                  CHECK(hs.xSplit && hs.xWarp && ns >= 2 && (n1 << lg) <= hs.xThreads, "split x");
+                  CHECK(hs.xSmem == xw_smem(ns, ilog2(n1), lg, bs, true, true) &&
+                        hs.xSmem == h.xSmem - (P / 2) * (size_t)(n1 + 4) * bs, "split smem");
+                  CHECK(((P / 2) * (size_t)(n1 + 4) * bs) % 16 == 0, "split halves on 16-byte boundaries");
+                }
               }
           }
         }

@@ -18,10 +18,12 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("form,plan", [("fp64", None), ("fp32", None), ("fp32", "x=2,w=1"),
-                                       ("fp32", "x=2,w=0")])
+                                       ("fp32", "x=2,w=0"), ("fp32", "x=2,w=2")])
 def test_bounded_wait_timeout_is_reported_and_context_recovers(native_lib, monkeypatch, form, plan):
     """Every x-pass kernel that waits on a bulk copy: the block-team (FP64 and
-    FP32 table form) and the warp-team (FP32 table form) kernels."""
+    FP32 table form) and the warp-team (FP32 table form, whole and split B
+    block: with the first half's wait run out, no second half is loaded)
+    kernels."""
     spec = workloads.SolveSpec(n=(32, 16, 16), ns=3, steps=6, sigma_max=0.05,
                                loops=[workloads.Loop(1, (16, 8, 8), 5.0)], noise_seed=8)
     x0, b0 = workloads.initial_state(spec)
@@ -31,7 +33,8 @@ def test_bounded_wait_timeout_is_reported_and_context_recovers(native_lib, monke
     s = native.solver_for(spec, form)
     if plan:
         monkeypatch.delenv("PFDD_PLAN")
-        assert s.plan()["x_pass"]["warp_teams"] == int(plan.endswith("w=1"))
+        assert s.plan()["x_pass"]["warp_teams"] == int(not plan.endswith("w=0"))
+        assert s.plan()["x_pass"]["b_split"] == int(plan.endswith("w=2"))
     try:
         s.set_state(x0, b0)
         monkeypatch.setenv("PFDD_TEST_DROP_BULK", "1")

@@ -200,3 +200,24 @@ def test_every_radix_plan_matches_oracle(native_lib, precision):
             assert np.max(np.abs(g[:, 0] - go) / np.abs(go)) <= gtol, (zn, yn)
             seen.add(x.tobytes())
     assert len(seen) >= 2  # the plans really differ in rounding
+
+
+@pytest.mark.parametrize("n,ns,plan", [((32, 16, 8), 12, "x=2,w=2"), ((64, 8, 16), 12, "x=1,w=2"),
+                                       ((128, 8, 16), 12, "x=2,w=2"), ((256, 8, 16), 12, "x=1,w=2"),
+                                       ((128, 16, 8), 3, "x=1,w=2"), ((256, 4, 8), 5, "x=1,w=2")])
+def test_split_b_block_same_bits(native_lib, n, ns, plan):
+    """The warp-team x-pass on the mirrored B(k) tile table with the tile's B
+    block in two halves of its pair rows through one buffer (the second half
+    loaded once every thread is past the first) gives the bits of the
+    whole-block kernel: mirrored pairs, Nyquist single lines, a CTA per pair
+    and per line, odd pair counts (5 systems: 15 pairs), 3 and 12 systems."""
+    spec = workloads.SolveSpec(n=n, ns=ns, steps=6, sigma_max=0.05, noise_seed=35,
+                               loops=workloads.random_loops(n, 3, 1.0, 3.0, ns, seed=35))
+    whole = plan.replace("w=2", "w=1")
+    g1, x1, p1 = pinned(spec, "fp32", plan)
+    g0, x0, p0 = pinned(spec, "fp32", whole)
+    assert p1["x_pass"]["b_split"] == 1 and p0["x_pass"]["b_split"] == 0
+    assert p1["x_pass"]["warp_teams"] == p0["x_pass"]["warp_teams"] == 1
+    assert p1["x_pass"]["smem"] < p0["x_pass"]["smem"]
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(x1, x0)
