@@ -221,3 +221,23 @@ def test_split_b_block_same_bits(native_lib, n, ns, plan):
     assert p1["x_pass"]["smem"] < p0["x_pass"]["smem"]
     np.testing.assert_array_equal(g1, g0)
     np.testing.assert_array_equal(x1, x0)
+
+
+def test_split_b_block_batched_pinned_and_idle(native_lib):
+    """The split B block on a batch of three with an idle replica (its CTAs
+    leave before the buffer swap) and pinned points: the bits of the
+    whole-block kernel."""
+    n = (256, 4, 8)
+    spec = workloads.SolveSpec(n=n, ns=12, steps=6, sigma_max=0.05, noise_seed=37,
+                               loops=workloads.random_loops(n, 3, 1.0, 3.0, 12, seed=37))
+
+    def prep(s, b0):
+        bc = np.zeros((3,) + b0.shape); bc[:, :, 0, 0, :] = 1.0
+        s.set_state(s.get_state(), bc)
+        s.set_active(1, False)
+
+    res = [pinned(spec, "fp32", plan, nrep=3, prepare=prep) for plan in ("x=1,w=2", "x=1,w=1")]
+    assert res[0][2]["x_pass"]["b_split"] == 1 and res[1][2]["x_pass"]["b_split"] == 0
+    live = [0, 2]
+    np.testing.assert_array_equal(res[0][0][:, live], res[1][0][:, live])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
