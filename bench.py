@@ -280,6 +280,21 @@ def time_e2e(native, workloads, spec, prec, K, device):
     L = s.L
     dp = C.POINTER(C.c_double)
     ptr = lambda t: C.cast(t.data_ptr(), dp)
+    # the host link as this process sees it (pinned copies of the state's size, one way each), so
+    # that the end-to-end figure can be read against it: it moves 1.2 GB a solve
+    link = {}
+    dev_buf = torch.empty(RF * N * 2, dtype=torch.float64, device=f"cuda:{device}")
+    for name, dst, src in (("h2d_gbs", dev_buf, xi_h), ("d2h_gbs", out_h, dev_buf)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        b.record()
+        b.synchronize()
+        link[name] = round(3 * RF * N * 16 / a.elapsed_time(b) / 1e6, 1)
+    del dev_buf
     # warm the path once (allocations of the first call are not part of a solve)
     L.pfdd_set_state(s.h, ptr(xi_h), ptr(bc_h))
     L.pfdd_step(s.h, 2, tau.ctypes.data_as(dp), g.ctypes.data_as(dp), ga.ctypes.data_as(dp))
@@ -298,7 +313,7 @@ def time_e2e(native, workloads, spec, prec, K, device):
     if st != 0:
         raise RuntimeError("e2e call failed")
     xi_bytes = RF * N * 16
-    return dict(ms=ms, h2d=(2 * xi_bytes) / K + RF * 8, d2h=xi_bytes / K + (RF + 1) * 8)
+    return dict(ms=ms, h2d=(2 * xi_bytes) / K + RF * 8, d2h=xi_bytes / K + (RF + 1) * 8, link=link)
 
 
 def cpu_baseline_port(spec, B, K_sample=2):
@@ -580,7 +595,7 @@ def run_ours(a):
         e = time_e2e(native, workloads, spec, head, K, dev)
         ems = dist.max(e["ms"])
         e2e = {"value": aggregate(dist.world, K, ems), "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
-               "d2h_bytes_per_step": e["d2h"],
+               "d2h_bytes_per_step": e["d2h"], "host_link": e["link"],
                "what": "pfdd_set_state (xi + xi_bc from pinned host) + pfdd_step(K) (stresses in, gamma out) "
                        "+ pfdd_get_state (xi to pinned host)"}
     # roofline of the dominant kernel of the headline form
