@@ -21,6 +21,9 @@ RUNNER = LIBDIR / "pfdd_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
+# per-unit flags: the z-pass's global loads (its S lines, read once) bypass L1
+# (measured at 128^3 x 12: 257.9 -> 254.9 us a launch)
+UNIT_FLAGS = {"pfdd_zpass.cu": ["-Xptxas", "-dlcm=cg"]}
 
 CU_SOURCES = ["pfdd_api.cu", "pfdd_fftpass.cu", "pfdd_zpass.cu", "pfdd_xpass_f32.cu", "pfdd_xpass_f64.cu", "pfdd_xpass_f32b.cu",
               "pfdd_xpass_warp.cu", "pfdd_noalloc.cu"]
@@ -57,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     jobs = []
     for src in CU_SOURCES:
         obj = objdir / (Path(src).stem + ".o")
-        jobs.append([nvcc, *NVFLAGS, "-c", str(CSRC / src), "-o", str(obj)])
+        jobs.append([nvcc, *NVFLAGS, *UNIT_FLAGS.get(src, []), "-c", str(CSRC / src), "-o", str(obj)])
     for src in C_SOURCES:
         obj = objdir / (Path(src).stem + ".o")
         jobs.append(["gcc", "-O2", "-fPIC", "-std=c11", "-I", str(ROOT / "include"), "-c", str(CSRC / src),
