@@ -2,7 +2,7 @@
 summation (avestrain F:641-749 for the plane sums, ResidualEnergy F:3920-3945
 for the line), from Re xi of a state.
 
-TEST INFRASTRUCTURE ONLY: the checker of the diagnostics tests; the product
+TEST INFRASTRUCTURE ONLY: the oracle of the diagnostics tests; the product
 never imports it."""
 import numpy as np
 
