@@ -358,12 +358,20 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
     from pfdd_gb300 import serve
     reqs = workloads.config4_requests(scale_steps=scale)
     # one seeded initial state per (grid, systems) class, reused by the class's
-    # requests: a step's cost does not depend on the values of xi
-    inputs = {}
+    # requests: a step's cost does not depend on the values of xi.  The client
+    # holds them in pinned host memory (pageable buffers are read by the GPU at
+    # the host link's speed only while their page translations are warm: cold,
+    # a 3.2 GB 256^3 x 12 state took about 1 s to upload instead of 16 ms)
+    import torch
+    inputs, pinned = {}, []
     for sp in reqs:
         key = (sp.n, sp.ns)
         if key not in inputs:
-            inputs[key] = native._interleave(workloads.initial_state(sp)[0].reshape(sp.ns, -1))
+            arr = native._interleave(workloads.initial_state(sp)[0].reshape(sp.ns, -1))
+            buf = torch.empty(arr.shape, dtype=torch.float64, pin_memory=True)
+            buf.numpy()[...] = arr
+            pinned.append(buf)
+            inputs[key] = buf.numpy()
     eps = {ns: native.fcc_eps(ns) for ns in {sp.ns for sp in reqs}}
 
     def submit(srv, sp):
