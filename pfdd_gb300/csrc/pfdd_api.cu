@@ -896,11 +896,27 @@ extern "C" pfdd_status pfdd_set_params(pfdd_ctx *c, const double *cd2, const dou
 // Upload xi (and the pinned mask) of replicas [r0, r0+nr).  xi_bc is staged
 // through the spectral buffer S (invalidated by a state change anyway) in
 // chunks and packed to bits on the device, so no host pass over it is needed.
+// A host <-> device copy of a state in pieces of 64 MB, each waited for before
+// the next is queued: the copy engines take copies in the order they are
+// queued, so a 3.2 GB state copied in one piece holds up every small copy of
+// the other contexts on the device (the server's other classes) until it is
+// done; in pieces those go through in between.
+static cudaError_t copy_in_pieces(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+  constexpr size_t kPiece = (size_t)64 << 20;
+  for (size_t off = 0; off < bytes; off += kPiece) {
+    const size_t n = std::min(kPiece, bytes - off);
+    cudaError_t e = cudaMemcpyAsync(static_cast<char *>(dst) + off, static_cast<const char *>(src) + off, n, kind, st);
+    if (e == cudaSuccess && off + n < bytes) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 static pfdd_status upload_state(pfdd_ctx *c, int r0, int nr, const double *xi, const double *bc) {
   CK(c, cudaSetDevice(c->dev));
   const size_t fieldN = (size_t)c->N, RFn = (size_t)nr * c->ns;
-  CK(c, cudaMemcpyAsync(c->xi + (size_t)r0 * c->ns * fieldN, xi, RFn * fieldN * sizeof(double2),
-                        cudaMemcpyHostToDevice, c->st));
+  CK(c, copy_in_pieces(c->xi + (size_t)r0 * c->ns * fieldN, xi, RFn * fieldN * sizeof(double2),
+                       cudaMemcpyHostToDevice, c->st));
   const size_t total_bits = (size_t)c->nrep * c->ns * fieldN, words = (total_bits + 31) / 32;
   if (bc && !c->bc) {
     CK(c, cudaMalloc(&c->bc, words * 4));
@@ -916,7 +932,7 @@ static pfdd_status upload_state(pfdd_ctx *c, int r0, int nr, const double *xi, c
     const size_t chunk = (size_t)c->nrep * c->ns * fieldN * vsize_of(c->prec) / (2 * sizeof(double));
     for (size_t off = 0; off < count; off += chunk) {
       const size_t n = std::min(chunk, count - off);
-      if (bc) CK(c, cudaMemcpyAsync(c->S, bc + 2 * off, n * 2 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+      if (bc) CK(c, copy_in_pieces(c->S, bc + 2 * off, n * 2 * sizeof(double), cudaMemcpyHostToDevice, c->st));
       pack_bc_kernel<<<1216, kThreads, 0, c->st>>>((const double *)c->S, (long long)n, (long long)(b0 + off), c->bc);
       CK(c, cudaGetLastError());
     }
@@ -1677,7 +1693,7 @@ extern "C" pfdd_status pfdd_state_diagnostics(pfdd_ctx *c, double *out) {
 extern "C" pfdd_status pfdd_get_state(pfdd_ctx *c, double *xi) {
   if (!c || !xi) return fail(c, PFDD_EINVAL, "pfdd_get_state: null argument");
   CK(c, cudaSetDevice(c->dev));
-  CK(c, cudaMemcpyAsync(xi, c->xi, (size_t)c->nrep * c->ns * c->N * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(c, copy_in_pieces(xi, c->xi, (size_t)c->nrep * c->ns * c->N * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
   CK(c, cudaStreamSynchronize(c->st));
   return PFDD_OK;
 }
@@ -1686,7 +1702,7 @@ extern "C" pfdd_status pfdd_get_replica_state(pfdd_ctx *c, int r, double *xi) {
   if (!c || !xi || r < 0 || r >= c->nrep) return fail(c, PFDD_EINVAL, "pfdd_get_replica_state: bad argument");
   CK(c, cudaSetDevice(c->dev));
   const size_t fl = (size_t)c->ns * c->N;
-  CK(c, cudaMemcpyAsync(xi, c->xi + (size_t)r * fl, fl * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
+  CK(c, copy_in_pieces(xi, c->xi + (size_t)r * fl, fl * sizeof(double2), cudaMemcpyDeviceToHost, c->st));
   CK(c, cudaStreamSynchronize(c->st));
   return PFDD_OK;
 }
