@@ -865,8 +865,12 @@ extern "C" pfdd_status pfdd_build_B(pfdd_ctx *c, double C11, double C12, double 
   CK(c, cudaMalloc(&dp, sizeof hp));
   cudaError_t e = cudaMemcpyAsync(dp, &hp, sizeof hp, cudaMemcpyHostToDevice, c->st);
   if (e == cudaSuccess) {
-    build_B_kernel<<<1216, 128, 0, c->st>>>(dp, c->bl, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
-                                            c->prec == PFDD_FP64 ? nullptr : (float *)c->B);
+    // a block per 128 points (each CTA short): a grid of SM-long CTAs would hold
+    // every SM for the whole build (46 ms at 256^3 x 12), and other contexts'
+    // kernels, whatever their stream priority, would wait for it
+    const long long blocks = std::min<long long>((c->N + 127) / 128, 0x7fffffffLL);
+    build_B_kernel<<<(unsigned)blocks, 128, 0, c->st>>>(dp, c->bl, c->prec == PFDD_FP64 ? (double *)c->B : nullptr,
+                                                        c->prec == PFDD_FP64 ? nullptr : (float *)c->B);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
