@@ -301,19 +301,24 @@ def time_e2e(native, workloads, spec, prec, K, device):
     stream = torch.cuda.ExternalStream(s.stream, device=f"cuda:{device}")
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    st = L.pfdd_set_state(s.h, ptr(xi_h), ptr(bc_h))
-    st |= L.pfdd_step(s.h, K, tau.ctypes.data_as(dp), g.ctypes.data_as(dp), ga.ctypes.data_as(dp))
-    st |= L.pfdd_get_state(s.h, ptr(out_h))
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
+    # the whole solve three times; the median is reported (one ~17 ms solve at K = 20
+    # is exposed to a single host-side hiccup)
+    runs, st = [], 0
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st |= L.pfdd_set_state(s.h, ptr(xi_h), ptr(bc_h))
+        st |= L.pfdd_step(s.h, K, tau.ctypes.data_as(dp), g.ctypes.data_as(dp), ga.ctypes.data_as(dp))
+        st |= L.pfdd_get_state(s.h, ptr(out_h))
+        e1.record(stream)
+        e1.synchronize()
+        runs.append(e0.elapsed_time(e1))
     s.close()
     if st != 0:
         raise RuntimeError("e2e call failed")
     xi_bytes = RF * N * 16
-    return dict(ms=ms, h2d=(2 * xi_bytes) / K + RF * 8, d2h=xi_bytes / K + (RF + 1) * 8, link=link)
+    return dict(ms=statistics.median(runs), runs_ms=[round(v, 3) for v in runs],
+                h2d=(2 * xi_bytes) / K + RF * 8, d2h=xi_bytes / K + (RF + 1) * 8, link=link)
 
 
 def cpu_baseline_port(spec, B, K_sample=2):
@@ -603,9 +608,9 @@ def run_ours(a):
         e = time_e2e(native, workloads, spec, head, K, dev)
         ems = dist.max(e["ms"])
         e2e = {"value": aggregate(dist.world, K, ems), "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
-               "d2h_bytes_per_step": e["d2h"], "host_link": e["link"],
+               "d2h_bytes_per_step": e["d2h"], "host_link": e["link"], "solves_ms": e["runs_ms"],
                "what": "pfdd_set_state (xi + xi_bc from pinned host) + pfdd_step(K) (stresses in, gamma out) "
-                       "+ pfdd_get_state (xi to pinned host)"}
+                       "+ pfdd_get_state (xi to pinned host); the median of three such solves"}
     # roofline of the dominant kernel of the headline form
     peaks = load_peaks()
     ks = rh["kstats"]
