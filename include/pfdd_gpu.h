@@ -138,9 +138,8 @@ pfdd_status pfdd_step(pfdd_ctx *ctx, int nsteps, const double *tau, double *gamm
  * error, the steps of the chunks completed before it).  The
  * pass marks carry over between calls, so a loop may be run in pieces.  The
  * state after the call is the state after the last step that ran: steps run
- * in chunks, and a chunk that ran past the stop is rewound (a device copy of
- * xi taken at its start) and run again up to the stop, which gives the same
- * bits. */
+ * in chunks no longer than the fewest steps to the next possible stop, so no
+ * chunk runs past it. */
 pfdd_status pfdd_converge_reset(pfdd_ctx *ctx, double gamma_prev);
 pfdd_status pfdd_step_converge(pfdd_ctx *ctx, int max_steps, const double *tau, double *gamma, double *gamma_a,
                                int *steps_done);

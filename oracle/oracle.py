@@ -170,6 +170,19 @@ def converge_stop(gamma: np.ndarray, gamma_prev: float = 0.0) -> int | None:
     return None
 
 
+def converge_min_steps(passed, count: int) -> int:
+    """The fewest further steps after which the loop of :func:`converge_stop`
+    can stop, given the pass marks of the steps so far and the count: 5 - count
+    with a full window of passes behind (29 or more), 34 - run otherwise, 35
+    when the count is past 5 (the bound pfdd_step_converge sizes its chunks by)."""
+    r = 0
+    while r < 29 and r < len(passed) and passed[len(passed) - 1 - r]:
+        r += 1
+    if r >= 29:
+        return 5 - count if count < 5 else 35
+    return 34 - r
+
+
 def strain_stress(n, xi: np.ndarray, eps: np.ndarray, C11: float, C12: float, C44: float, sigma_app: np.ndarray,
                   d=(1.0, 1.0, 1.0)):
     """Strain and stress fields of state ``xi`` (complex [ns, n1, n2, n3]):

@@ -442,12 +442,10 @@ struct pfdd_ctx {
   int diag_steps = 0;
   // the inner loop's convergence stop (plasticconverge, F:3732-3785): which
   // steps of the current loop passed the change test, the run of full 30-step
-  // windows, the loop's step count and the previous gamma; and a copy of xi
-  // to rewind a chunk that ran past the stop (pfdd_step_converge)
+  // windows, the loop's step count and the previous gamma (pfdd_step_converge)
   std::vector<uint8_t> cv_test;
   int cv_count = 0, cv_it = 0;
   double cv_last = 0.0;
-  double2 *xi_snap = nullptr;
 };
 
 // wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
@@ -724,7 +722,7 @@ extern "C" void pfdd_destroy(pfdd_ctx *c) {
   void *dp[] = {c->S, c->xi, c->bc, c->B, c->tau, c->part, c->gam_a, c->gam, c->tau_field, c->dslip_dev,
                 c->active, c->flag, c->errflag, c->step_ctr, c->tw[0], c->tw[1], c->tw[2],
                 c->xt, c->xtoff, c->xline, c->xord, c->sp_E, c->sp_eps, c->sp_sig, c->sp_part, c->sp_dp,
-                c->d_dpts, c->d_dgat, c->xi_snap};
+                c->d_dpts, c->d_dgat};
   if (c->sp_plan) pfdd_fft_plan_destroy(c->sp_plan);
   if (c->h_errflag) cudaFreeHost(c->h_errflag);
   for (auto &ev : c->tm.pool) cudaEventDestroy(ev);
@@ -1564,6 +1562,20 @@ static bool converge_update(pfdd_ctx *c, double g) {
   return stop;
 }
 
+// The fewest further steps after which the loop can stop: a count is taken
+// only by a passing step whose last 30 steps all passed, and a passing step
+// with a shorter run of passes resets it.  With a run of r passing steps
+// behind and the count at k, every step passing from here on: 5 - k steps
+// when the window is already full (r >= 29, k < 5), else 29 - r steps to fill
+// it and 5 to count (a count past 5, after a stop, must first be reset: a
+// failing step and 34 more).
+static int converge_min_steps(const pfdd_ctx *c) {
+  int r = 0;
+  while (r < 29 && r < c->cv_it && c->cv_test[c->cv_it - 1 - r]) ++r;
+  if (r >= 29) return c->cv_count < 5 ? 5 - c->cv_count : 35;
+  return 34 - r;
+}
+
 extern "C" pfdd_status pfdd_converge_reset(pfdd_ctx *c, double gamma_prev) {
   if (!c) return PFDD_EINVAL;
   c->cv_test.clear();
@@ -1581,38 +1593,27 @@ extern "C" pfdd_status pfdd_step_converge(pfdd_ctx *c, int max_steps, const doub
   *steps_done = 0;
   if (max_steps == 0) return PFDD_OK;
   if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_step_converge: state not set");
-  CK(c, cudaSetDevice(c->dev));
-  const size_t xbytes = (size_t)c->ns * c->N * sizeof(double2);
-  if (!c->xi_snap) CK(c, cudaMalloc(&c->xi_snap, xbytes));
   const int ns = c->ns;
   int done = 0;
   while (done < max_steps) {
-    const int k = std::min(c->kchunk, max_steps - done);
-    CK(c, cudaMemcpyAsync(c->xi_snap, c->xi, xbytes, cudaMemcpyDeviceToDevice, c->st));
+    // a chunk no longer than the fewest steps to the next possible stop: the
+    // loop can stop at its last step at the earliest, never inside it
+    const int k = std::min({c->kchunk, max_steps - done, converge_min_steps(c)});
     double *ga = gamma_a ? gamma_a + (size_t)done * ns : nullptr;
-    pfdd_status st = pfdd_step(c, k, tau + (size_t)done * ns, gamma + done, ga);
+    const pfdd_status st = pfdd_step(c, k, tau + (size_t)done * ns, gamma + done, ga);
     if (st != PFDD_OK) {
       *steps_done = done;  // the chunks before this one
       return st;
     }
     int stop = -1;
-    for (int j = 0; j < k && stop < 0; ++j)
+    for (int j = 0; j < k; ++j)
       if (converge_update(c, gamma[done + j])) stop = j;
-    if (stop < 0) {
-      done += k;
-      continue;
+    done += k;
+    if (stop >= 0 && stop != k - 1) {
+      *steps_done = done;
+      return fail(c, PFDD_EINVAL, "pfdd_step_converge: stop at step %d inside a chunk of %d", done - k + stop, k);
     }
-    if (stop < k - 1) {  // rewind to the chunk's start and run exactly to the stop (same bits)
-      CK(c, cudaMemcpyAsync(c->xi, c->xi_snap, xbytes, cudaMemcpyDeviceToDevice, c->st));
-      c->specValid = false;
-      st = pfdd_step(c, stop + 1, tau + (size_t)done * ns, gamma + done, ga);
-      if (st != PFDD_OK) {
-        *steps_done = done;
-        return st;
-      }
-    }
-    done += stop + 1;
-    break;
+    if (stop >= 0) break;
   }
   *steps_done = done;
   return PFDD_OK;

@@ -47,3 +47,46 @@ def test_oracle_trajectory_stops_at_the_same_step():
 ])
 def test_rule_cases(seq, prev, want):
     assert oracle.converge_stop(seq, prev) == want
+
+
+def _rule_states(seq, prev):
+    """(pass marks so far, count, stopped) before each step of the rule."""
+    passed, count, last, out = [], 0, float(prev), []
+    for it, g in enumerate(map(float, seq)):
+        out.append((list(passed), count))
+        ok = (abs((g - last) / g) < 1e-8 or abs(g) < 1e-12) if g != 0 else (abs(g - last) < 1e-15 or abs(g) < 1e-14)
+        passed.append(ok)
+        if ok and it >= 29:
+            if all(passed[it - 29:it + 1]):
+                count += 1
+            elif count != 0:
+                count = 0
+        if count == 5:
+            count += 1
+        last = g
+    return out
+
+
+def test_chunks_never_pass_the_stop():
+    """pfdd_step_converge runs chunks no longer than the fewest steps to the next
+    possible stop: on random pass patterns (runs of constant gamma between jumps,
+    and the reference golden's gammas) no stop ever falls before that bound."""
+    rng = np.random.default_rng(7)
+    seqs = [load_golden(CASE)[1]["gamma"]]
+    for _ in range(300):
+        seq, g = [], 1e-3
+        for _ in range(int(rng.integers(20, 200))):
+            if rng.random() < rng.uniform(0.0, 0.15):
+                g *= 1.0 + rng.uniform(1e-6, 1e-2)
+            seq.append(g)
+        seqs.append(np.array(seq))
+    for seq in seqs:
+        states = _rule_states(seq, 0.0)
+        stop = oracle.converge_stop(seq, 0.0)
+        for i, (passed, count) in enumerate(states):
+            if stop is not None and i >= stop:
+                break
+            k = oracle.converge_min_steps(passed, count)
+            assert k >= 1
+            if stop is not None:
+                assert i + k <= stop, (i, k, stop)
