@@ -144,6 +144,19 @@ pfdd_status pfdd_converge_reset(pfdd_ctx *ctx, double gamma_prev);
 pfdd_status pfdd_step_converge(pfdd_ctx *ctx, int max_steps, const double *tau, double *gamma, double *gamma_a,
                                int *steps_done);
 
+/* The same for every replica of a batched context, each with its own test
+ * and stop: pfdd_converge_reset_batched takes gamma_prev[nrep] (and
+ * pfdd_converge_reset sets all replicas alike); pfdd_step_converge_batched
+ * takes tau[max_steps][nrep][ns] and writes gamma[max_steps][nrep],
+ * gamma_a[max_steps][nrep][ns] (may be NULL) and steps_done[nrep].  The
+ * active replicas take part; one that stops leaves the batch (idle, its state
+ * that of its stop step) and is active again when the call returns; idle
+ * replicas are left alone (steps_done 0).  Chunks end at the first possible
+ * stop of any running replica. */
+pfdd_status pfdd_converge_reset_batched(pfdd_ctx *ctx, const double *gamma_prev);
+pfdd_status pfdd_step_converge_batched(pfdd_ctx *ctx, int max_steps, const double *tau, double *gamma,
+                                       double *gamma_a, int *steps_done);
+
 /* Copies xi of every replica back: xi[nrep][ns][N][2]. */
 pfdd_status pfdd_get_state(pfdd_ctx *ctx, double *xi);
 pfdd_status pfdd_get_replica_state(pfdd_ctx *ctx, int r, double *xi);

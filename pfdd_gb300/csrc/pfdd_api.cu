@@ -360,6 +360,69 @@ struct KTiming {
 
 }  // namespace
 
+// The state of one inner loop's convergence test: which of its steps passed
+// the change test, the count of passing steps with a full window behind,
+// the loop's step count and the previous gamma.
+struct ConvergeTracker {
+  std::vector<uint8_t> test;
+  int count = 0, it = 0;
+  double last = 0.0;
+
+  void reset(double gamma_prev) {
+    test.clear();
+    count = 0;
+    it = 0;
+    last = gamma_prev;
+  }
+
+  // plasticconverge (F:3732-3785) for the gamma of one more step: the step
+  // passes when gamma changed by less than 1e-8 relative (1e-15 absolute when
+  // gamma is 0) or |gamma| < 1e-12 (1e-14); a passing step whose last 30 steps
+  // all passed adds one to the count, one whose window is not full resets it
+  // (a failing step leaves it); the loop stops when the count reaches 5.
+  // True: the loop stops after this step.
+  bool update(double g) {
+    bool passed;
+    if (g != 0) {
+      const double r = (g - last) / g;
+      passed = (r < 0 ? -r : r) < 1E-8 || (g > 0 ? g : -g) < 1E-12;
+    } else {
+      const double d = g - last;
+      passed = (d < 0 ? -d : d) < 1E-15 || (g > 0 ? g : -g) < 1E-14;
+    }
+    if ((int)test.size() <= it) test.resize((size_t)it + 1, 0);
+    if (passed) {
+      test[it] = 1;
+      if (it >= 29) {
+        int t = 0;
+        for (int i = 0; i < 30; ++i) t += test[it - i];
+        if (t == 30) count++;
+        else if (count != 0) count = 0;
+      }
+    }
+    bool stop = false;
+    if (count == 5) {
+      count++;
+      stop = true;
+    }
+    last = g;
+    it++;
+    return stop;
+  }
+
+  // The fewest further steps after which the loop can stop: with a run of r
+  // passing steps behind and the count at k, every step passing from here on,
+  // 5 - k steps when the window is already full (r >= 29, k < 5), else 29 - r
+  // steps to fill it and 5 to count (a count past 5, after a stop, must first
+  // be reset: a failing step and 34 more).
+  int min_steps() const {
+    int r = 0;
+    while (r < 29 && r < it && test[it - 1 - r]) ++r;
+    if (r >= 29) return count < 5 ? 5 - count : 35;
+    return 34 - r;
+  }
+};
+
 struct pfdd_ctx {
   int n[3] = {0, 0, 0};
   int ns = 0, nrep = 0, prec = 0, dev = 0;
@@ -440,12 +503,9 @@ struct pfdd_ctx {
   double *d_dgat = nullptr;
   std::vector<double> h_dgat, h_diag;
   int diag_steps = 0;
-  // the inner loop's convergence stop (plasticconverge, F:3732-3785): which
-  // steps of the current loop passed the change test, the run of full 30-step
-  // windows, the loop's step count and the previous gamma (pfdd_step_converge)
-  std::vector<uint8_t> cv_test;
-  int cv_count = 0, cv_it = 0;
-  double cv_last = 0.0;
+  // the inner loop's convergence stop (plasticconverge, F:3732-3785), one
+  // tracker a replica (pfdd_step_converge, pfdd_step_converge_batched)
+  std::vector<ConvergeTracker> cv;
 };
 
 // wait limit of the bounded device waits under PFDD_TEST_DROP_BULK (the normal
@@ -1525,63 +1585,21 @@ extern "C" pfdd_status pfdd_step(pfdd_ctx *c, int nsteps, const double *tau, dou
                               : run_steps<float>(c, nsteps, tau, gamma, gamma_a);
 }
 
-// plasticconverge (F:3732-3785) for the gamma of one more step of the inner
-// loop: the step passes when gamma changed by less than 1e-8 relative (1e-15
-// absolute when gamma is 0) or |gamma| < 1e-12 (1e-14); a passing step whose
-// last 30 steps all passed extends the run of full windows, one whose window
-// is not full resets it (a failing step leaves it); the loop stops when the
-// run reaches 5.  True: the loop stops after this step.
-static bool converge_update(pfdd_ctx *c, double g) {
-  const double gl = c->cv_last;
-  bool passed;
-  if (g != 0) {
-    const double r = (g - gl) / g;
-    passed = (r < 0 ? -r : r) < 1E-8 || (g > 0 ? g : -g) < 1E-12;
-  } else {
-    const double d = g - gl;
-    passed = (d < 0 ? -d : d) < 1E-15 || (g > 0 ? g : -g) < 1E-14;
-  }
-  const int it = c->cv_it;
-  if ((int)c->cv_test.size() <= it) c->cv_test.resize((size_t)it + 1, 0);
-  if (passed) {
-    c->cv_test[it] = 1;
-    if (it >= 29) {
-      int t = 0;
-      for (int i = 0; i < 30; ++i) t += c->cv_test[it - i];
-      if (t == 30) c->cv_count++;
-      else if (c->cv_count != 0) c->cv_count = 0;
-    }
-  }
-  bool stop = false;
-  if (c->cv_count == 5) {
-    c->cv_count++;
-    stop = true;
-  }
-  c->cv_last = g;
-  c->cv_it++;
-  return stop;
-}
-
-// The fewest further steps after which the loop can stop: a count is taken
-// only by a passing step whose last 30 steps all passed, and a passing step
-// with a shorter run of passes resets it.  With a run of r passing steps
-// behind and the count at k, every step passing from here on: 5 - k steps
-// when the window is already full (r >= 29, k < 5), else 29 - r steps to fill
-// it and 5 to count (a count past 5, after a stop, must first be reset: a
-// failing step and 34 more).
-static int converge_min_steps(const pfdd_ctx *c) {
-  int r = 0;
-  while (r < 29 && r < c->cv_it && c->cv_test[c->cv_it - 1 - r]) ++r;
-  if (r >= 29) return c->cv_count < 5 ? 5 - c->cv_count : 35;
-  return 34 - r;
+static void ensure_trackers(pfdd_ctx *c) {
+  if ((int)c->cv.size() != c->nrep) c->cv.assign(c->nrep, ConvergeTracker());
 }
 
 extern "C" pfdd_status pfdd_converge_reset(pfdd_ctx *c, double gamma_prev) {
   if (!c) return PFDD_EINVAL;
-  c->cv_test.clear();
-  c->cv_count = 0;
-  c->cv_it = 0;
-  c->cv_last = gamma_prev;
+  ensure_trackers(c);
+  for (auto &t : c->cv) t.reset(gamma_prev);
+  return PFDD_OK;
+}
+
+extern "C" pfdd_status pfdd_converge_reset_batched(pfdd_ctx *c, const double *gamma_prev) {
+  if (!c || !gamma_prev) return fail(c, PFDD_EINVAL, "pfdd_converge_reset_batched: null argument");
+  ensure_trackers(c);
+  for (int r = 0; r < c->nrep; ++r) c->cv[r].reset(gamma_prev[r]);
   return PFDD_OK;
 }
 
@@ -1590,33 +1608,73 @@ extern "C" pfdd_status pfdd_step_converge(pfdd_ctx *c, int max_steps, const doub
   if (!c || max_steps < 0 || (max_steps > 0 && (!tau || !gamma)) || !steps_done)
     return fail(c, PFDD_EINVAL, "pfdd_step_converge: bad argument");
   if (c->nrep != 1) return fail(c, PFDD_EINVAL, "pfdd_step_converge: one solve per context (nrep == 1)");
-  *steps_done = 0;
+  return pfdd_step_converge_batched(c, max_steps, tau, gamma, gamma_a, steps_done);
+}
+
+extern "C" pfdd_status pfdd_step_converge_batched(pfdd_ctx *c, int max_steps, const double *tau, double *gamma,
+                                                  double *gamma_a, int *steps_done) {
+  if (!c || max_steps < 0 || (max_steps > 0 && (!tau || !gamma)) || !steps_done)
+    return fail(c, PFDD_EINVAL, "pfdd_step_converge_batched: bad argument");
+  const int R = c->nrep, ns = c->ns;
+  for (int r = 0; r < R; ++r) steps_done[r] = 0;
   if (max_steps == 0) return PFDD_OK;
-  if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_step_converge: state not set");
-  const int ns = c->ns;
+  if (!c->hasState) return fail(c, PFDD_ENOTREADY, "pfdd_step_converge_batched: state not set");
+  ensure_trackers(c);
+  // the replicas that take part: the active ones; each leaves (idle, its state
+  // kept) at its stop, and the ones that left are active again at the end
+  std::vector<uint8_t> run(R, 0), left(R, 0);
+  for (int r = 0; r < R; ++r) run[r] = c->h_active[r];
+  std::vector<double> g, ga;
   int done = 0;
+  pfdd_status st = PFDD_OK;
   while (done < max_steps) {
-    // a chunk no longer than the fewest steps to the next possible stop: the
-    // loop can stop at its last step at the earliest, never inside it
-    const int k = std::min({c->kchunk, max_steps - done, converge_min_steps(c)});
-    double *ga = gamma_a ? gamma_a + (size_t)done * ns : nullptr;
-    const pfdd_status st = pfdd_step(c, k, tau + (size_t)done * ns, gamma + done, ga);
-    if (st != PFDD_OK) {
-      *steps_done = done;  // the chunks before this one
-      return st;
+    // a chunk no longer than the fewest steps to any running replica's next
+    // possible stop: a replica can stop at its last step at the earliest
+    int k = std::min(c->kchunk, max_steps - done), nrun = 0;
+    for (int r = 0; r < R; ++r)
+      if (run[r]) {
+        k = std::min(k, c->cv[r].min_steps());
+        ++nrun;
+      }
+    if (!nrun) break;
+    g.assign((size_t)k * R, 0.0);
+    ga.assign((size_t)k * R * ns, 0.0);
+    st = pfdd_step(c, k, tau + (size_t)done * R * ns, g.data(), ga.data());
+    if (st != PFDD_OK) break;
+    for (int r = 0; r < R; ++r) {
+      if (!run[r]) continue;
+      int stop = -1;
+      for (int j = 0; j < k; ++j) {
+        gamma[(size_t)(done + j) * R + r] = g[(size_t)j * R + r];
+        if (gamma_a)
+          for (int a = 0; a < ns; ++a)
+            gamma_a[((size_t)(done + j) * R + r) * ns + a] = ga[((size_t)j * R + r) * ns + a];
+        if (c->cv[r].update(g[(size_t)j * R + r])) stop = j;
+      }
+      steps_done[r] = done + k;
+      if (stop >= 0 && stop != k - 1) {
+        st = fail(c, PFDD_EINVAL, "pfdd_step_converge: replica %d stops at step %d inside a chunk of %d", r,
+                  done + stop, k);
+        break;
+      }
+      if (stop >= 0) {
+        run[r] = 0;
+        if (R > 1) {
+          st = pfdd_set_replica_active(c, r, 0);
+          if (st != PFDD_OK) break;
+          left[r] = 1;
+        }
+      }
     }
-    int stop = -1;
-    for (int j = 0; j < k; ++j)
-      if (converge_update(c, gamma[done + j])) stop = j;
+    if (st != PFDD_OK) break;
     done += k;
-    if (stop >= 0 && stop != k - 1) {
-      *steps_done = done;
-      return fail(c, PFDD_EINVAL, "pfdd_step_converge: stop at step %d inside a chunk of %d", done - k + stop, k);
-    }
-    if (stop >= 0) break;
   }
-  *steps_done = done;
-  return PFDD_OK;
+  for (int r = 0; r < R; ++r)
+    if (left[r]) {
+      const pfdd_status e = pfdd_set_replica_active(c, r, 1);
+      if (st == PFDD_OK) st = e;
+    }
+  return st;
 }
 
 extern "C" pfdd_status pfdd_get_plan(pfdd_ctx *c, char *buf, size_t len) {

@@ -33,7 +33,7 @@ EXPORTS = [
     "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
     "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority", "pfdd_get_plan",
     "pfdd_strain_stress", "pfdd_set_diagnostics", "pfdd_get_diagnostics", "pfdd_state_diagnostics",
-    "pfdd_converge_reset", "pfdd_step_converge",
+    "pfdd_converge_reset", "pfdd_step_converge", "pfdd_converge_reset_batched", "pfdd_step_converge_batched",
 ]
 
 DIAG_COLUMNS = ("energy_in", "energy_in2", "energy_in3", "energy_in4", "energy_Residual", "energy_intotal")
@@ -100,6 +100,8 @@ def load():
     L.pfdd_step.argtypes = [vp, i, dp, dp, dp]
     L.pfdd_converge_reset.argtypes = [vp, d]
     L.pfdd_step_converge.argtypes = [vp, i, dp, dp, dp, C.POINTER(C.c_int)]
+    L.pfdd_converge_reset_batched.argtypes = [vp, dp]
+    L.pfdd_step_converge_batched.argtypes = [vp, i, dp, dp, dp, C.POINTER(C.c_int)]
     L.pfdd_get_state.argtypes = [vp, dp]
     L.pfdd_get_replica_state.argtypes = [vp, i, dp]
     L.pfdd_set_replica_active.argtypes = [vp, i, i]
@@ -292,6 +294,23 @@ class Solver:
                     "pfdd_step_converge")
         k = done.value
         return g[:k].copy(), ga[:k].copy()
+
+    def converge_reset_batched(self, gamma_prev):
+        """Per-replica start of an inner loop: gamma_prev [nrep]."""
+        gp = _f64(np.broadcast_to(np.asarray(gamma_prev, dtype=np.float64), (self.nrep,)))
+        self._check(self.L.pfdd_converge_reset_batched(self.h, _dp(gp)), "pfdd_converge_reset_batched")
+
+    def step_converge_batched(self, tau: np.ndarray):
+        """Every active replica's inner loop with its own stop: tau [K, nrep, ns].
+        Returns (steps run [nrep], gamma [K, nrep], gamma_a [K, nrep, ns]); a
+        replica's entries past its stop are zero."""
+        t = _f64(np.asarray(tau).reshape(-1, self.nrep, self.ns))
+        K = t.shape[0]
+        g = np.zeros((K, self.nrep)); ga = np.zeros((K, self.nrep, self.ns))
+        done = (C.c_int * self.nrep)()
+        self._check(self.L.pfdd_step_converge_batched(self.h, K, _dp(t), _dp(g), _dp(ga), done),
+                    "pfdd_step_converge_batched")
+        return np.array(list(done)), g, ga
 
     def get_state(self) -> np.ndarray:
         x = np.zeros((self.nrep, self.ns, self.N, 2))

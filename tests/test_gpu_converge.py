@@ -99,3 +99,34 @@ def test_batched_context_is_rejected(native_lib):
         assert ei.value.status == native.PFDD_EINVAL
     finally:
         s.close()
+
+
+def test_batched_loops_stop_each_at_its_own_step(native_lib, monkeypatch):
+    """Three replicas in one context, each with its own convergence test: two
+    of the golden solve (the reference stops it at 112 steps) and one with
+    ten times its noise, which stops later. Each replica stops where a
+    one-solve context stops on its input, with the same bits; the replica that
+    stops first leaves the batch at its stop while the other runs on."""
+    spec, z = load_golden(CASE)
+    loud = workloads.SolveSpec(**{**spec.__dict__, "noise_amp": spec.noise_amp * 10})
+    monkeypatch.setenv("PFDD_NO_TUNE", "1")  # one launch plan in every context: the same rounding
+    singles = [_run(sp, "fp64") for sp in (spec, loud)]
+    assert len(singles[0][0]) == int(z["steps_run"]) < len(singles[1][0]) < spec.steps
+    x0, b0 = workloads.initial_state(spec)
+    x1, _ = workloads.initial_state(loud)
+    tau = native.spec_tau(spec)
+    s = native.solver_for(spec, "fp64", nrep=3)
+    try:
+        s.set_state(np.stack([x0, x1, x0]), np.stack([b0] * 3))
+        s.converge_reset(0.0)
+        done, g, ga = s.step_converge_batched(np.stack([tau] * 3, axis=1))
+        x = s.get_state().reshape(3, spec.ns, -1)
+    finally:
+        s.close()
+    for r, (sg, sga, sx) in zip((0, 1, 2), (singles[0], singles[1], singles[0])):
+        k = len(sg)
+        assert done[r] == k, (r, done)
+        np.testing.assert_array_equal(g[:k, r], sg)
+        np.testing.assert_array_equal(ga[:k, r], sga)
+        assert not g[k:, r].any()
+        np.testing.assert_array_equal(x[r], sx)
