@@ -20,7 +20,9 @@
  *     depend on what else runs beside it.
  *
  * Stresses follow the ramp of the workloads: step s (0-based) of a solve
- * applies tau_max[a] * ((s + 1.0) / steps).
+ * applies tau_max[a] * ((s + 1.0) / steps).  A converging solve (converge
+ * set) ends at its loop's stop if that comes first: its slot's chunks are cut
+ * to the fewest steps to that stop, so it is never run past it.
  *
  * Scheduling: free slots take the class's shortest queued solve first; class
  * streams get CUDA priorities by the size of one solve's step (grid points x
@@ -54,6 +56,10 @@ typedef struct {
   const double *xi;               /* [ns][N][2] initial order parameter */
   const double *xi_bc;            /* [ns][N][2] pinned flags, or NULL: every point evolves */
   double *xi_out;                 /* [ns][N][2] receives the final xi, or NULL */
+  int converge;                   /* nonzero: the solve also ends where the reference's convergence test
+                                     ends its inner loop (plasticconverge, F:3732-3785), as
+                                     pfdd_step_converge does; `steps` stays the ramp's length */
+  double gamma_prev;              /* with converge: the gamma its first step is compared with (F:4575) */
 } pfdd_request;
 
 /* precision: PFDD_FP64, PFDD_FFT_FP32 or PFDD_FFT_FP32_BFLY.  hbm_budget: device
@@ -72,6 +78,11 @@ pfdd_status pfdd_server_submit(pfdd_server *srv, const pfdd_request *req, long l
  * xi_out).  Outputs (each may be NULL): gamma [steps], gamma_a [steps][ns] and
  * the time from submit to completion in seconds.  Returns the solve's status. */
 pfdd_status pfdd_server_wait(pfdd_server *srv, long long id, double *gamma, double *gamma_a, double *latency_s);
+
+/* The same, and the number of steps the solve ran (`steps`, or fewer for a
+ * converging solve that stopped; gamma and gamma_a hold zeros beyond it). */
+pfdd_status pfdd_server_wait_run(pfdd_server *srv, long long id, double *gamma, double *gamma_a, double *latency_s,
+                                 int *steps_run);
 
 /* Totals since creation: solve steps executed, solves finished, classes
  * created, peak device bytes reserved. */

@@ -39,6 +39,7 @@
 #include <thread>
 #include <vector>
 
+#include "pfdd_converge.h"
 #include "pfdd_gpu.h"
 #include "pfdd_serve.h"
 
@@ -58,6 +59,8 @@ struct Request {
   std::string key;
   std::vector<double> gamma, gamma_a;
   int progress = 0;
+  pfdd::ConvergeTracker cv;  // converging solves: the loop's test
+  bool stopped = false;      // converging solves: the test ended the loop
   Clock::time_point t_submit, t_done;
   bool done = false;
   pfdd_status status = PFDD_OK;
@@ -305,6 +308,7 @@ static void worker_main(pfdd_server *s, Class *c) {
         act[r] = c->slot[r] >= 0 ? s->reqs.at(c->slot[r]).get() : nullptr;
         if (act[r]) {
           chunk = std::min(chunk, act[r]->spec.steps - act[r]->progress);
+          if (act[r]->spec.converge) chunk = std::min(chunk, act[r]->cv.min_steps());  // never past a stop
           ++nact;
         }
       }
@@ -332,19 +336,25 @@ static void worker_main(pfdd_server *s, Class *c) {
       for (int r = 0; r < R; ++r) {
         Request *q = act[r];
         if (!q) continue;
+        pfdd_status eq = e;
         for (int k = 0; k < chunk; ++k) {
           q->gamma[q->progress + k] = g[(size_t)k * R + r];
           for (int a = 0; a < ns; ++a)
             q->gamma_a[(size_t)(q->progress + k) * ns + a] = ga[((size_t)k * R + r) * ns + a];
+          if (q->spec.converge && eq == PFDD_OK && q->cv.update(g[(size_t)k * R + r])) {
+            if (k != chunk - 1) eq = PFDD_EINVAL;  // a stop inside a chunk: the bound failed
+            q->stopped = true;
+          }
         }
         q->progress += chunk;
         s->steps_done += chunk;
-        if (e != PFDD_OK || q->progress >= q->spec.steps) finished.push_back(r);
+        if (eq != PFDD_OK || q->stopped || q->progress >= q->spec.steps) finished.push_back(r);
+        if (eq != PFDD_OK) q->status = eq;
       }
     }
     for (int r : finished) {
       Request *q = act[r];
-      pfdd_status e2 = e;
+      pfdd_status e2 = e != PFDD_OK ? e : q->status;
       if (e2 == PFDD_OK && q->spec.xi_out) e2 = pfdd_get_replica_state(c->ctx, r, q->spec.xi_out);
       pfdd_set_replica_active(c->ctx, r, 0);
       std::lock_guard<std::mutex> lk(s->mu);
@@ -396,6 +406,7 @@ extern "C" pfdd_status pfdd_server_submit(pfdd_server *s, const pfdd_request *q,
   r->key = class_key(*q);
   r->gamma.assign(q->steps, 0.0);
   r->gamma_a.assign((size_t)q->steps * q->ns, 0.0);
+  if (q->converge) r->cv.reset(q->gamma_prev);
   std::vector<std::thread> done_workers;
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -415,6 +426,11 @@ extern "C" pfdd_status pfdd_server_submit(pfdd_server *s, const pfdd_request *q,
 
 extern "C" pfdd_status pfdd_server_wait(pfdd_server *s, long long id, double *gamma, double *gamma_a,
                                         double *latency_s) {
+  return pfdd_server_wait_run(s, id, gamma, gamma_a, latency_s, nullptr);
+}
+
+extern "C" pfdd_status pfdd_server_wait_run(pfdd_server *s, long long id, double *gamma, double *gamma_a,
+                                            double *latency_s, int *steps_run) {
   if (!s) return PFDD_EINVAL;
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(id);
@@ -424,6 +440,7 @@ extern "C" pfdd_status pfdd_server_wait(pfdd_server *s, long long id, double *ga
   if (gamma) std::memcpy(gamma, r.gamma.data(), r.gamma.size() * sizeof(double));
   if (gamma_a) std::memcpy(gamma_a, r.gamma_a.data(), r.gamma_a.size() * sizeof(double));
   if (latency_s) *latency_s = std::chrono::duration<double>(r.t_done - r.t_submit).count();
+  if (steps_run) *steps_run = r.progress;
   const pfdd_status st = r.status;
   s->reqs.erase(it);
   return st;

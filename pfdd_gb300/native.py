@@ -31,6 +31,7 @@ EXPORTS = [
     "pfdd_fft_backward", "pfdd_status_string", "pfdd_frec", "pfdd_setfcc", "pfdd_setorient", "pfdd_seteps",
     "pfdd_resolve_shear", "pfdd_ramp_tau", "pfdd_get_stream", "pfdd_set_kernel_timing", "pfdd_kernel_stat",
     "pfdd_fft_device_noalloc", "pfdd_server_create", "pfdd_server_submit", "pfdd_server_wait",
+    "pfdd_server_wait_run",
     "pfdd_server_stats", "pfdd_server_destroy", "pfdd_set_stream_priority", "pfdd_get_plan",
     "pfdd_strain_stress", "pfdd_set_diagnostics", "pfdd_get_diagnostics", "pfdd_state_diagnostics",
     "pfdd_converge_reset", "pfdd_step_converge", "pfdd_converge_reset_batched", "pfdd_step_converge_batched",
@@ -143,6 +144,7 @@ def load():
     L.pfdd_server_create.argtypes = [C.POINTER(vp), i, i, sz, i, i]
     L.pfdd_server_submit.argtypes = [vp, vp, C.POINTER(ll)]
     L.pfdd_server_wait.argtypes = [vp, ll, dp, dp, dp]
+    L.pfdd_server_wait_run.argtypes = [vp, ll, dp, dp, dp, C.POINTER(C.c_int)]
     L.pfdd_server_stats.argtypes = [vp, C.POINTER(ll), C.POINTER(ll), C.POINTER(ll), C.POINTER(sz)]
     L.pfdd_server_destroy.argtypes = [vp]
     L.pfdd_server_destroy.restype = None

@@ -28,6 +28,7 @@ class _Request(C.Structure):
         ("d1", C.c_double), ("d2", C.c_double), ("d3", C.c_double),
         ("eps", C.POINTER(C.c_double)), ("tau_max", C.POINTER(C.c_double)),
         ("xi", C.POINTER(C.c_double)), ("xi_bc", C.POINTER(C.c_double)), ("xi_out", C.POINTER(C.c_double)),
+        ("converge", C.c_int), ("gamma_prev", C.c_double),
     ]
 
 
@@ -37,6 +38,7 @@ class Result:
     gamma: np.ndarray     # [steps]
     gamma_a: np.ndarray   # [steps, ns]
     latency_s: float      # submit -> completion
+    steps_run: int = 0    # steps the solve ran (fewer than steps when a converging solve stopped)
 
 
 class Server:
@@ -56,7 +58,7 @@ class Server:
     def submit_raw(self, n, ns: int, steps: int, C11: float, C12: float, C44: float, eps: np.ndarray,
                    tau_max: np.ndarray, xi: np.ndarray, bc: Optional[np.ndarray] = None, cd2: float = 0.01,
                    asf: float = 0.1, dslip: float = 1.0, uq2: float = 1.0, d=(1.0, 1.0, 1.0),
-                   want_xi: bool = True) -> int:
+                   want_xi: bool = True, converge: bool = False, gamma_prev: float = 0.0) -> int:
         """Queues a solve from raw inputs.  xi is complex [ns, ...] or already
         interleaved float64 [ns, N, 2]; the arrays are held until :meth:`wait`."""
         n = tuple(int(v) for v in n)
@@ -74,7 +76,7 @@ class Server:
         out = np.empty((ns, N, 2)) if want_xi else None
         q = _Request(n[0], n[1], n[2], int(ns), int(steps), C11, C12, C44, cd2, asf, dslip, uq2,
                      float(d[0]), float(d[1]), float(d[2]), native._dp(e), native._dp(t), native._dp(x),
-                     native._dp(b), native._dp(out))
+                     native._dp(b), native._dp(out), int(bool(converge)), float(gamma_prev))
         rid = C.c_longlong()
         st = self.L.pfdd_server_submit(self.h, C.byref(q), C.byref(rid))
         if st != native.PFDD_OK:
@@ -82,25 +84,26 @@ class Server:
         self._held[rid.value] = (ns, steps, x, b, out)  # the server reads/writes these until wait
         return rid.value
 
-    def submit(self, spec: workloads.SolveSpec) -> int:
-        """Queues one :class:`SolveSpec` (FCC slip systems, sigma_xz ramp)."""
+    def submit(self, spec: workloads.SolveSpec, converge: bool = False) -> int:
+        """Queues one :class:`SolveSpec` (FCC slip systems, sigma_xz ramp); with
+        ``converge`` the solve also ends at the reference's convergence stop."""
         eps = native.fcc_eps(spec.ns, dslip=spec.dslip)
         sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
         tau_max = native.resolved_shear(eps, sig)
         xi, bc = workloads.initial_state(spec)
         C44, C12 = spec.mu, spec.lam
         return self.submit_raw(spec.n, spec.ns, spec.steps, 2.0 * C44 + C12, C12, C44, eps, tau_max, xi, bc,
-                               cd2=spec.cd2, asf=spec.asf, dslip=spec.dslip, uq2=1.0, d=spec.d)
+                               cd2=spec.cd2, asf=spec.asf, dslip=spec.dslip, uq2=1.0, d=spec.d, converge=converge)
 
     def wait(self, rid: int) -> Result:
         ns, steps, _, _, out = self._held[rid]
-        g = np.zeros(steps); ga = np.zeros((steps, ns)); lat = C.c_double()
-        st = self.L.pfdd_server_wait(self.h, rid, native._dp(g), native._dp(ga), C.byref(lat))
+        g = np.zeros(steps); ga = np.zeros((steps, ns)); lat = C.c_double(); ran = C.c_int()
+        st = self.L.pfdd_server_wait_run(self.h, rid, native._dp(g), native._dp(ga), C.byref(lat), C.byref(ran))
         del self._held[rid]
         if st != native.PFDD_OK:
             raise native.PFDDError(st, f"pfdd_server_wait: {self.L.pfdd_status_string(st).decode()}")
         xi = None if out is None else out[..., 0] + 1j * out[..., 1]
-        return Result(xi, g, ga, lat.value)
+        return Result(xi, g, ga, lat.value, ran.value)
 
     def stats(self) -> dict:
         a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong(); p = C.c_size_t()

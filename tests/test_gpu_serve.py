@@ -67,3 +67,42 @@ def test_budget_serialises_classes_and_rejects_oversize(native_lib):
         x, g, _ = solo(sp, "fp32")
         np.testing.assert_array_equal(r.xi, x)
         np.testing.assert_array_equal(r.gamma, g)
+
+
+def test_converging_solves_stop_where_the_reference_stops(native_lib):
+    """Solves submitted with the convergence stop end where the reference's test
+    ends the inner loop: the golden solve (the reference stops it after 112 of
+    its 300 steps) and the same with ten times its noise (it stops later), beside
+    a fixed-length solve of the same class. Each has the bits of a one-solve
+    context on its input (pfdd_step_converge for the two, pfdd_step for the
+    other), and the converging ones hold zeros past their stop."""
+    from conftest import load_golden
+    spec, z = load_golden("converge_16c_ns3_cd01")
+    loud = workloads.SolveSpec(**{**spec.__dict__, "noise_amp": spec.noise_amp * 10})
+    fixed = workloads.SolveSpec(**{**spec.__dict__, "steps": 60, "noise_seed": 11})
+    with serve.Server("fp64", max_slots=3, chunk_steps=7) as srv:
+        ids = [srv.submit(spec, converge=True), srv.submit(fixed), srv.submit(loud, converge=True)]
+        res = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    assert st["classes_created"] == 1
+    for sp, r in ((spec, res[0]), (loud, res[2])):
+        s = native.solver_for(sp, "fp64")
+        try:
+            x0, b0 = workloads.initial_state(sp)
+            s.set_state(x0, b0)
+            s.converge_reset(0.0)
+            g, ga = s.step_converge(native.spec_tau(sp))
+            x = s.get_state()[0].reshape(sp.ns, -1)
+        finally:
+            s.close()
+        k = len(g)
+        assert r.steps_run == k < sp.steps
+        np.testing.assert_array_equal(r.gamma[:k], g)
+        np.testing.assert_array_equal(r.gamma_a[:k], ga)
+        assert not r.gamma[k:].any()
+        np.testing.assert_array_equal(r.xi, x)
+    assert res[0].steps_run == int(z["steps_run"]) < res[2].steps_run
+    x, g, ga = solo(fixed, "fp64")
+    assert res[1].steps_run == fixed.steps
+    np.testing.assert_array_equal(res[1].gamma, g)
+    np.testing.assert_array_equal(res[1].xi, x)
