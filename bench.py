@@ -66,7 +66,8 @@ def parse():
 # distributed plumbing (replicas only)
 
 class Dist:
-    def __init__(self, want: int):
+    def __init__(self, want: int, backend: str | None = None):
+        """backend: None picks nccl when a GPU is visible, else gloo."""
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -75,7 +76,8 @@ class Dist:
             import torch
             import torch.distributed as dist
             os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend is None:
+                backend = "nccl" if torch.cuda.is_available() else "gloo"
             if backend == "nccl":
                 torch.cuda.set_device(self.local)
             dist.init_process_group(backend)

@@ -20,7 +20,7 @@ def _worker(rank, world, port, q):
     os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
                       MASTER_PORT=str(port))
     import bench
-    d = bench.Dist(world)
+    d = bench.Dist(world, backend="gloo")  # CPU ranks, also where a GPU is visible
     d.barrier()
     my_ms = 100.0 + 50.0 * rank          # rank 1 is the slow one
     mx = d.max(my_ms)
