@@ -46,6 +46,8 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
                                step) and ebarrier_full.dat (one line per inner TDGL
                                step): the step, energy_in, energy_in2, energy_in3,
                                energy_in4, energy_Residual, energy_intotal
+14  4269-4271                  grid spacing d1, d2, d3 from -D (the reference fixes
+                               them at 1; frec and Bmatrix take them)
 ==  =========================  ====================================================
 """
 from __future__ import annotations
@@ -95,6 +97,15 @@ DEFAULTS_BLOCK = r"""
 #endif
 #ifndef PFDD_BDIV
 #define PFDD_BDIV sqrt(2.0)
+#endif
+#ifndef PFDD_D1
+#define PFDD_D1 1.0
+#endif
+#ifndef PFDD_D2
+#define PFDD_D2 1.0
+#endif
+#ifndef PFDD_D3
+#define PFDD_D3 1.0
 #endif
 #ifndef PFDD_DIAG
 #define PFDD_DIAG 1
@@ -155,6 +166,9 @@ PATCHES = [
      "GG = calloc((size_t)(2*(NS)*(NS)*(N1)*(N2)*(N3)), sizeof(double));"),
     (4186, "choice=1;", "choice=2;"),
     (4205, "plastic_max =3000;", "plastic_max =pfdd_krun_(PFDD_K);"),
+    (4269, "d1 = 1;", "d1 = PFDD_D1;"),
+    (4270, "d2 = 1;", "d2 = PFDD_D2;"),
+    (4271, "d3 = 1;", "d3 = PFDD_D3;"),
     (4278, "Asf2[is] = 0.0262;", "Asf2[is] = PFDD_ASF;"),
     (4280, "Asf2[0] = 0.0064659518668288441;", "Asf2[0] = PFDD_ASF;"),
     (4281, "Asf2[1] = 0.0064659518668288441;", "Asf2[1] = PFDD_ASF;"),
@@ -203,31 +217,35 @@ def write_patched_source(src: Path = REF_SRC, dst: Path = PATCHED) -> Path:
     return dst
 
 
-def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01, strain=False) -> str:
+def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01, strain=False,
+                d=(1.0, 1.0, 1.0)) -> str:
     tag = "x".join(str(int(v)) for v in n)
-    return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}_{'fp64' if fp64 else 'fp32'}"
+    dtag = "" if tuple(map(float, d)) == (1.0, 1.0, 1.0) else "_d" + "x".join(f"{float(v):g}" for v in d)
+    return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}{dtag}_{'fp64' if fp64 else 'fp32'}"
             f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}{'_strain' if strain else ''}")
 
 
 def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=True,
-                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False) -> Path:
-    """strain=True (implies diag): strain.txt, stress.txt and the full-precision
-    strain/stress dumps of the initial state (patch 12)."""
+                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False, d=(1.0, 1.0, 1.0)) -> Path:
+    """Compile one configuration of the patched reference; returns the binary path.
+    strain=True (implies diag): strain.txt, stress.txt and the full-precision
+    strain/stress dumps of the initial state (patch 12).  d: the grid spacing
+    (patch 14)."""
     diag = diag or strain
-    """Compile one configuration of the patched reference; returns the binary path."""
     if REF_SRC.exists() and (force or not PATCHED.exists()
                              or PATCHED.stat().st_mtime < Path(__file__).stat().st_mtime):
         write_patched_source()
     if not PATCHED.exists():
         raise FileNotFoundError("patched reference source missing (no reference checkout here)")
-    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain)
+    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d)
     if out.exists() and out.stat().st_mtime >= PATCHED.stat().st_mtime and not force:
         return out
     defs = [f"-DPFDD_N1={n[0]}", f"-DPFDD_N2={n[1]}", f"-DPFDD_N3={n[2]}", f"-DPFDD_K={k}",
             f"-DPFDD_SIGMA={sigma!r}", f"-DPFDD_ASF={asf!r}", f"-DPFDD_CD2={cd2!r}",
             f"-DPFDD_MU={mu!r}", f"-DPFDD_LAMBDA={lam!r}",
             f"-DPFDD_DIAG={1 if diag else 0}", f"-DPFDD_SETUP_B={1 if setup_b else 0}",
-            f"-DPFDD_STRAIN_OUT={1 if strain else 0}"]
+            f"-DPFDD_STRAIN_OUT={1 if strain else 0}",
+            f"-DPFDD_D1={float(d[0])!r}", f"-DPFDD_D2={float(d[1])!r}", f"-DPFDD_D3={float(d[2])!r}"]
     if fp64:
         defs.append("-Dfloat=double")
     cmd = ["gcc", "-O2", "-w", "-DUSE_FOURN", *defs]

@@ -45,6 +45,12 @@ def cases():
         n=(8, 8, 8), ns=12, steps=30, sigma_max=0.08,
         loops=workloads.random_loops((8, 8, 8), 3, 1.5, 3.0, 12, seed=11), noise_seed=11)
     yield "config1_64c_ns12_k10", workloads.config1(steps=10, n=64)
+    # anisotropic grid spacing (frec divides by d per axis, so B(k) changes) with
+    # material and kinetic constants other than the defaults
+    yield "fcc12_32x8x16_aniso_k30", workloads.SolveSpec(
+        n=(32, 8, 16), ns=12, steps=30, sigma_max=0.05,
+        loops=workloads.random_loops((32, 8, 16), 3, 2.0, 4.0, 12, seed=21), noise_seed=21,
+        nu=0.25, asf=0.15, cd2=0.02, d=(1.0, 0.5, 2.0))
 
 
 def spec_json(spec: workloads.SolveSpec) -> str:
@@ -54,7 +60,7 @@ def spec_json(spec: workloads.SolveSpec) -> str:
 
 def run_case(name: str, spec: workloads.SolveSpec, fp64: bool, krun: int | None = None):
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=fp64,
-                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)

@@ -242,6 +242,20 @@ def test_fp32_form_error_vs_fp64_oracle(native_lib):
     assert np.max(np.abs(xf - xo)) <= 1e-5
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp32_bfly"])
+def test_fp32_forms_with_anisotropic_spacing(native_lib, precision):
+    """Grid spacing d = (1, 0.5, 2) (frec divides each axis's frequency by its
+    spacing, so B(k) changes) with nu, Asf and CD2 off their defaults: the FP32
+    table form (B(k) built in FP64, rounded) and the closed-form one (B(k)
+    evaluated in FP32 from the frequencies) against the reference's own FP64
+    run of the same solve, at the FP32-form bar."""
+    spec, z = load_golden("fcc12_32x8x16_aniso_k30")
+    assert spec.d == (1.0, 0.5, 2.0)
+    xf, g, _, _ = run_gpu(spec, precision)
+    assert rel(g, z["gamma"]) <= FP32_GAMMA_RTOL
+    assert np.max(np.abs(xf.reshape(spec.ns, -1) - z["xi_final"])) <= 1e-5
+
+
 def test_nonfinite_state_is_reported(native_lib):
     spec = workloads.SolveSpec(n=(8, 8, 8), ns=3, steps=3, sigma_max=0.0, noise_seed=0)
     s = native.solver_for(spec)
