@@ -72,6 +72,8 @@ class SolveSpec:
     dslip: float = 1.0
     d: Tuple[float, float, float] = (1.0, 1.0, 1.0)
     name: str = ""
+    pin_frac: float = 0.0     # fraction of every field's points held fixed (xi_bc = 1)
+    pin_seed: int = 0
 
     @property
     def lam(self) -> float:
@@ -103,7 +105,10 @@ def initial_state(spec: SolveSpec):
     """Return ``(xi, xi_bc)`` as complex128 / float64 arrays of shape ``[ns, n1, n2, n3]``.
 
     Re(xi) = 1 inside each loop of its system, plus U(-amp, amp) noise on Re of every
-    field (PCG64, ``noise_seed``); Im(xi) = 0; every point evolves (xi_bc = 0)."""
+    field (PCG64, ``noise_seed``); Im(xi) = 0.  Every point evolves (xi_bc = 0) unless
+    ``pin_frac`` > 0: then each point of each field is held fixed (xi_bc = 1, the
+    reference's obstacle marking, skipped by plasticevolv's test at F:3482) with that
+    probability (PCG64, ``pin_seed``)."""
     n1, n2, n3 = spec.n
     re = np.zeros((spec.ns, n1, n2, n3), dtype=np.float64)
     for lp in spec.loops:
@@ -114,6 +119,9 @@ def initial_state(spec: SolveSpec):
         re += rng.uniform(-spec.noise_amp, spec.noise_amp, size=re.shape)
     xi = re.astype(np.complex128)
     bc = np.zeros((spec.ns, n1, n2, n3), dtype=np.float64)
+    if spec.pin_frac > 0:
+        rng = np.random.Generator(np.random.PCG64(np.random.SeedSequence([spec.pin_seed, 2])))
+        bc[rng.random(bc.shape) < spec.pin_frac] = 1.0
     return xi, bc
 
 

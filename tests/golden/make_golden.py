@@ -51,6 +51,11 @@ def cases():
         n=(32, 8, 16), ns=12, steps=30, sigma_max=0.05,
         loops=workloads.random_loops((32, 8, 16), 3, 2.0, 4.0, 12, seed=21), noise_seed=21,
         nu=0.25, asf=0.15, cd2=0.02, d=(1.0, 0.5, 2.0))
+    # a tenth of every field's points held fixed (xi_bc = 1), some inside the loops
+    yield "fcc12_16c_pinned_k30", workloads.SolveSpec(
+        n=(16, 16, 16), ns=12, steps=30, sigma_max=0.06,
+        loops=workloads.random_loops((16, 16, 16), 4, 2.5, 5.0, 12, seed=31), noise_seed=31,
+        pin_frac=0.1, pin_seed=31)
 
 
 def spec_json(spec: workloads.SolveSpec) -> str:
