@@ -48,6 +48,8 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
                                energy_in4, energy_Residual, energy_intotal
 14  4269-4271                  grid spacing d1, d2, d3 from -D (the reference fixes
                                them at 1; frec and Bmatrix take them)
+15  4209                       slip-plane spacing dslip from -D (fixed at 1; the
+                               eigenstrains and tau/dslip take it)
 ==  =========================  ====================================================
 """
 from __future__ import annotations
@@ -100,6 +102,9 @@ DEFAULTS_BLOCK = r"""
 #endif
 #ifndef PFDD_D1
 #define PFDD_D1 1.0
+#endif
+#ifndef PFDD_DSLIP
+#define PFDD_DSLIP 1.0
 #endif
 #ifndef PFDD_D2
 #define PFDD_D2 1.0
@@ -166,6 +171,7 @@ PATCHES = [
      "GG = calloc((size_t)(2*(NS)*(NS)*(N1)*(N2)*(N3)), sizeof(double));"),
     (4186, "choice=1;", "choice=2;"),
     (4205, "plastic_max =3000;", "plastic_max =pfdd_krun_(PFDD_K);"),
+    (4209, "dslip = 1.0;", "dslip = PFDD_DSLIP;"),
     (4269, "d1 = 1;", "d1 = PFDD_D1;"),
     (4270, "d2 = 1;", "d2 = PFDD_D2;"),
     (4271, "d3 = 1;", "d3 = PFDD_D3;"),
@@ -218,26 +224,28 @@ def write_patched_source(src: Path = REF_SRC, dst: Path = PATCHED) -> Path:
 
 
 def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01, strain=False,
-                d=(1.0, 1.0, 1.0)) -> str:
+                d=(1.0, 1.0, 1.0), dslip=1.0) -> str:
     tag = "x".join(str(int(v)) for v in n)
     dtag = "" if tuple(map(float, d)) == (1.0, 1.0, 1.0) else "_d" + "x".join(f"{float(v):g}" for v in d)
+    dtag += "" if float(dslip) == 1.0 else f"_sl{float(dslip):g}"
     return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}{dtag}_{'fp64' if fp64 else 'fp32'}"
             f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}{'_strain' if strain else ''}")
 
 
 def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=True,
-                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False, d=(1.0, 1.0, 1.0)) -> Path:
+                asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False, d=(1.0, 1.0, 1.0),
+                dslip=1.0) -> Path:
     """Compile one configuration of the patched reference; returns the binary path.
     strain=True (implies diag): strain.txt, stress.txt and the full-precision
     strain/stress dumps of the initial state (patch 12).  d: the grid spacing
-    (patch 14)."""
+    (patch 14); dslip: the slip-plane spacing (patch 15)."""
     diag = diag or strain
     if REF_SRC.exists() and (force or not PATCHED.exists()
                              or PATCHED.stat().st_mtime < Path(__file__).stat().st_mtime):
         write_patched_source()
     if not PATCHED.exists():
         raise FileNotFoundError("patched reference source missing (no reference checkout here)")
-    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d)
+    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d, dslip)
     if out.exists() and out.stat().st_mtime >= PATCHED.stat().st_mtime and not force:
         return out
     defs = [f"-DPFDD_N1={n[0]}", f"-DPFDD_N2={n[1]}", f"-DPFDD_N3={n[2]}", f"-DPFDD_K={k}",
@@ -245,7 +253,8 @@ def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=
             f"-DPFDD_MU={mu!r}", f"-DPFDD_LAMBDA={lam!r}",
             f"-DPFDD_DIAG={1 if diag else 0}", f"-DPFDD_SETUP_B={1 if setup_b else 0}",
             f"-DPFDD_STRAIN_OUT={1 if strain else 0}",
-            f"-DPFDD_D1={float(d[0])!r}", f"-DPFDD_D2={float(d[1])!r}", f"-DPFDD_D3={float(d[2])!r}"]
+            f"-DPFDD_D1={float(d[0])!r}", f"-DPFDD_D2={float(d[1])!r}", f"-DPFDD_D3={float(d[2])!r}",
+            f"-DPFDD_DSLIP={float(dslip)!r}"]
     if fp64:
         defs.append("-Dfloat=double")
     cmd = ["gcc", "-O2", "-w", "-DUSE_FOURN", *defs]

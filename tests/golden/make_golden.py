@@ -56,6 +56,10 @@ def cases():
         n=(16, 16, 16), ns=12, steps=30, sigma_max=0.06,
         loops=workloads.random_loops((16, 16, 16), 4, 2.5, 5.0, 12, seed=31), noise_seed=31,
         pin_frac=0.1, pin_seed=31)
+    # slip-plane spacing 2 (the eigenstrains b n / dslip and the update's tau / dslip)
+    yield "fcc12_16x32x8_dslip2_k30", workloads.SolveSpec(
+        n=(16, 32, 8), ns=12, steps=30, sigma_max=0.1,
+        loops=workloads.random_loops((16, 32, 8), 3, 2.0, 4.0, 12, seed=41), noise_seed=41, dslip=2.0)
 
 
 def spec_json(spec: workloads.SolveSpec) -> str:
@@ -65,7 +69,8 @@ def spec_json(spec: workloads.SolveSpec) -> str:
 
 def run_case(name: str, spec: workloads.SolveSpec, fp64: bool, krun: int | None = None):
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=fp64,
-                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d)
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d,
+                              dslip=spec.dslip)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)
