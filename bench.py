@@ -331,7 +331,7 @@ def cpu_baseline_port(spec, B, K_sample=2):
     tau = native.spec_tau(spec)[:K_sample]
     ns = spec.ns
     t0 = time.perf_counter()
-    oracle.run(spec.n, B, x0, b0, [spec.cd2] * ns, [spec.asf] * ns, [spec.dslip] * ns, 1.0, tau)
+    oracle.run(spec.n, B, x0, b0, [spec.cd2] * ns, [spec.asf] * ns, [spec.dslip] * ns, spec.uq2, tau)
     dt = time.perf_counter() - t0
     # oracle.run evaluates K_sample + 0 forces after the initial one: K_sample steps of work
     return {"value": K_sample / dt, "unit": "steps/s", "cores": oracle.nthreads(), "kind": "port",

@@ -50,6 +50,8 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
                                them at 1; frec and Bmatrix take them)
 15  4209                       slip-plane spacing dslip from -D (fixed at 1; the
                                eigenstrains and tau/dslip take it)
+16  4195                       uq2, the update's factor of the elastic force, from
+                               -D (fixed at 1)
 ==  =========================  ====================================================
 """
 from __future__ import annotations
@@ -105,6 +107,9 @@ DEFAULTS_BLOCK = r"""
 #endif
 #ifndef PFDD_DSLIP
 #define PFDD_DSLIP 1.0
+#endif
+#ifndef PFDD_UQ2
+#define PFDD_UQ2 1.0
 #endif
 #ifndef PFDD_D2
 #define PFDD_D2 1.0
@@ -170,6 +175,7 @@ PATCHES = [
     (4162, "GG = malloc((2*(NS)*(NS)*(N1)*(N2)*(N3))*sizeof(double));",
      "GG = calloc((size_t)(2*(NS)*(NS)*(N1)*(N2)*(N3)), sizeof(double));"),
     (4186, "choice=1;", "choice=2;"),
+    (4195, "uq2=1.0;", "uq2=PFDD_UQ2;"),
     (4205, "plastic_max =3000;", "plastic_max =pfdd_krun_(PFDD_K);"),
     (4209, "dslip = 1.0;", "dslip = PFDD_DSLIP;"),
     (4269, "d1 = 1;", "d1 = PFDD_D1;"),
@@ -224,28 +230,30 @@ def write_patched_source(src: Path = REF_SRC, dst: Path = PATCHED) -> Path:
 
 
 def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01, strain=False,
-                d=(1.0, 1.0, 1.0), dslip=1.0) -> str:
+                d=(1.0, 1.0, 1.0), dslip=1.0, uq2=1.0) -> str:
     tag = "x".join(str(int(v)) for v in n)
     dtag = "" if tuple(map(float, d)) == (1.0, 1.0, 1.0) else "_d" + "x".join(f"{float(v):g}" for v in d)
     dtag += "" if float(dslip) == 1.0 else f"_sl{float(dslip):g}"
+    dtag += "" if float(uq2) == 1.0 else f"_u{float(uq2):g}"
     return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}{dtag}_{'fp64' if fp64 else 'fp32'}"
             f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}{'_strain' if strain else ''}")
 
 
 def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=True,
                 asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False, d=(1.0, 1.0, 1.0),
-                dslip=1.0) -> Path:
+                dslip=1.0, uq2=1.0) -> Path:
     """Compile one configuration of the patched reference; returns the binary path.
     strain=True (implies diag): strain.txt, stress.txt and the full-precision
     strain/stress dumps of the initial state (patch 12).  d: the grid spacing
-    (patch 14); dslip: the slip-plane spacing (patch 15)."""
+    (patch 14); dslip: the slip-plane spacing (patch 15); uq2: the force factor
+    (patch 16)."""
     diag = diag or strain
     if REF_SRC.exists() and (force or not PATCHED.exists()
                              or PATCHED.stat().st_mtime < Path(__file__).stat().st_mtime):
         write_patched_source()
     if not PATCHED.exists():
         raise FileNotFoundError("patched reference source missing (no reference checkout here)")
-    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d, dslip)
+    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d, dslip, uq2)
     if out.exists() and out.stat().st_mtime >= PATCHED.stat().st_mtime and not force:
         return out
     defs = [f"-DPFDD_N1={n[0]}", f"-DPFDD_N2={n[1]}", f"-DPFDD_N3={n[2]}", f"-DPFDD_K={k}",
@@ -254,7 +262,7 @@ def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=
             f"-DPFDD_DIAG={1 if diag else 0}", f"-DPFDD_SETUP_B={1 if setup_b else 0}",
             f"-DPFDD_STRAIN_OUT={1 if strain else 0}",
             f"-DPFDD_D1={float(d[0])!r}", f"-DPFDD_D2={float(d[1])!r}", f"-DPFDD_D3={float(d[2])!r}",
-            f"-DPFDD_DSLIP={float(dslip)!r}"]
+            f"-DPFDD_DSLIP={float(dslip)!r}", f"-DPFDD_UQ2={float(uq2)!r}"]
     if fp64:
         defs.append("-Dfloat=double")
     cmd = ["gcc", "-O2", "-w", "-DUSE_FOURN", *defs]

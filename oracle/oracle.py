@@ -139,7 +139,8 @@ def solve(spec, steps: int | None = None, eps_bdiv: float = float(np.sqrt(2.0)))
     tau = ramp_tau(tau_max, spec.steps)[:K]
     xi, bc = workloads.initial_state(spec)
     ns = spec.ns
-    return run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf), np.full(ns, spec.dslip), 1.0, tau)
+    return run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf), np.full(ns, spec.dslip), spec.uq2,
+               tau)
 
 
 def converge_stop(gamma: np.ndarray, gamma_prev: float = 0.0) -> int | None:

@@ -93,7 +93,8 @@ class Server:
         xi, bc = workloads.initial_state(spec)
         C44, C12 = spec.mu, spec.lam
         return self.submit_raw(spec.n, spec.ns, spec.steps, 2.0 * C44 + C12, C12, C44, eps, tau_max, xi, bc,
-                               cd2=spec.cd2, asf=spec.asf, dslip=spec.dslip, uq2=1.0, d=spec.d, converge=converge)
+                               cd2=spec.cd2, asf=spec.asf, dslip=spec.dslip, uq2=spec.uq2, d=spec.d,
+                               converge=converge)
 
     def wait(self, rid: int) -> Result:
         ns, steps, _, _, out = self._held[rid]

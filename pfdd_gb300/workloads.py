@@ -74,6 +74,7 @@ class SolveSpec:
     name: str = ""
     pin_frac: float = 0.0     # fraction of every field's points held fixed (xi_bc = 1)
     pin_seed: int = 0
+    uq2: float = 1.0          # factor of the elastic force in the update (F:3488-3489)
 
     @property
     def lam(self) -> float:

@@ -60,6 +60,10 @@ def cases():
     yield "fcc12_16x32x8_dslip2_k30", workloads.SolveSpec(
         n=(16, 32, 8), ns=12, steps=30, sigma_max=0.1,
         loops=workloads.random_loops((16, 32, 8), 3, 2.0, 4.0, 12, seed=41), noise_seed=41, dslip=2.0)
+    # the update's factor of the elastic force (Re and Im) at 0.6
+    yield "fcc12_32x16x8_uq2_k30", workloads.SolveSpec(
+        n=(32, 16, 8), ns=12, steps=30, sigma_max=0.05,
+        loops=workloads.random_loops((32, 16, 8), 3, 2.0, 4.0, 12, seed=51), noise_seed=51, uq2=0.6)
 
 
 def spec_json(spec: workloads.SolveSpec) -> str:
@@ -70,7 +74,7 @@ def spec_json(spec: workloads.SolveSpec) -> str:
 def run_case(name: str, spec: workloads.SolveSpec, fp64: bool, krun: int | None = None):
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=fp64,
                               asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d,
-                              dslip=spec.dslip)
+                              dslip=spec.dslip, uq2=spec.uq2)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)
