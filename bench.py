@@ -385,9 +385,9 @@ def run_serving(native, workloads, dev, scale, load=0.7, max_slots=16, chunk_ste
         sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = sp.sigma_max
         tmax = native.resolved_shear(eps[sp.ns], sig)
         C44, C12 = sp.mu, sp.lam
-        return srv.submit_raw(sp.n, sp.ns, sp.steps, 2.0 * C44 + C12, C12, C44, eps[sp.ns], tmax,
+        return srv.submit_raw(sp.n, sp.ns, sp.steps, sp.C11, C12, C44, eps[sp.ns], tmax,
                               inputs[(sp.n, sp.ns)], None, cd2=sp.cd2, asf=sp.asf, dslip=sp.dslip,
-                              want_xi=False)
+                              uq2=sp.uq2, want_xi=False)
 
     # lone-solve step times per class: the one-at-a-time baselines
     solo = {}

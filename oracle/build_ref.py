@@ -27,7 +27,9 @@ Patch set (line numbers of ``PFDD_Final_GPU.c``):
 5   4580                       ``interfacevolv`` disabled (bimaterial special case)
 6   1432                       regression fix: the virtual DD term is not added to
                                slip row ``isb`` (the older program's semantics)
-7   302-304, 4278-4281, 4297   mu = C44, lambda = C12, Asf2 and CD2 from -D
+7   81, 302-304, 4278-4281,    mu = C44, lambda = C12, C11 (default 2 mu + lambda,
+    4297                       isotropic; a cubic C11 with material type MT 2),
+                               Asf2 and CD2 from -D
 8   3876-3877, 3484, 3488      applied sigma_xz = PFDD_SIGMA, ramped by
                                (it_plastic+1)/K inside ``plasticevolv``
 9   4442-4532, 4616-4645,      diagnostics that never feed xi (energies, strain,
@@ -111,6 +113,12 @@ DEFAULTS_BLOCK = r"""
 #ifndef PFDD_UQ2
 #define PFDD_UQ2 1.0
 #endif
+#ifndef PFDD_C11
+#define PFDD_C11 (2.0*PFDD_MU+PFDD_LAMBDA)
+#endif
+#ifndef PFDD_MT
+#define PFDD_MT 1
+#endif
 #ifndef PFDD_D2
 #define PFDD_D2 1.0
 #endif
@@ -143,13 +151,14 @@ static int pfdd_krun_(int k_) { const char *s_ = getenv("PFDD_KRUN"); return s_ 
 # (1-based line, original substring, replacement substring)
 PATCHES = [
     (26, "#include <sys/time.h>", "#include <sys/time.h>\n" + DEFAULTS_BLOCK),
+    (81, "#define MT 1", "#define MT PFDD_MT"),
     (82, "#define NMAT 2", "#define NMAT 1"),
     (83, "#define N1 32", "#define N1 PFDD_N1"),
     (84, "#define N2 2 ", "#define N2 PFDD_N2 "),
     (85, "#define N3 32", "#define N3 PFDD_N3"),
     (86, "#define NS1 1 ", "#define NS1 12 "),
     (91, "#define NTD 0/", "#define NTD 2/"),
-    (302, "mc->C11=168.4E9;", "mc->C11=2.0*PFDD_MU+PFDD_LAMBDA;"),
+    (302, "mc->C11=168.4E9;", "mc->C11=PFDD_C11;"),
     (303, "mc->C12=121.4E9;", "mc->C12=PFDD_LAMBDA;"),
     (304, "mc->C44=23.5E9;", "mc->C44=PFDD_MU;"),
     (818, "if(it == NT-NTD-1){",
@@ -230,30 +239,36 @@ def write_patched_source(src: Path = REF_SRC, dst: Path = PATCHED) -> Path:
 
 
 def binary_name(n, k, sigma, fp64=True, diag=False, setup_b=True, asf=0.1, cd2=0.01, strain=False,
-                d=(1.0, 1.0, 1.0), dslip=1.0, uq2=1.0) -> str:
+                d=(1.0, 1.0, 1.0), dslip=1.0, uq2=1.0, mu=1.0, lam=1.5, c11=None) -> str:
+    """A name for every value the build takes from -D (the values at their
+    defaults left out), so that a cached binary is never reused for another
+    configuration."""
     tag = "x".join(str(int(v)) for v in n)
     dtag = "" if tuple(map(float, d)) == (1.0, 1.0, 1.0) else "_d" + "x".join(f"{float(v):g}" for v in d)
     dtag += "" if float(dslip) == 1.0 else f"_sl{float(dslip):g}"
     dtag += "" if float(uq2) == 1.0 else f"_u{float(uq2):g}"
+    dtag += "" if float(mu) == 1.0 else f"_mu{float(mu)!r}"
+    dtag += "" if float(lam) == 1.5 else f"_la{float(lam)!r}"
+    dtag += "" if c11 is None else f"_C11{float(c11)!r}"
     return (f"pfdd_ref_{tag}_k{k}_s{sigma:g}_a{asf:g}_c{cd2:g}{dtag}_{'fp64' if fp64 else 'fp32'}"
             f"{'_diag' if diag else ''}{'' if setup_b else '_nob'}{'_strain' if strain else ''}")
 
 
 def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=True,
                 asf=0.1, cd2=0.01, mu=1.0, lam=1.5, force=False, strain=False, d=(1.0, 1.0, 1.0),
-                dslip=1.0, uq2=1.0) -> Path:
+                dslip=1.0, uq2=1.0, c11=None) -> Path:
     """Compile one configuration of the patched reference; returns the binary path.
     strain=True (implies diag): strain.txt, stress.txt and the full-precision
     strain/stress dumps of the initial state (patch 12).  d: the grid spacing
     (patch 14); dslip: the slip-plane spacing (patch 15); uq2: the force factor
-    (patch 16)."""
+    (patch 16); c11: C11 when it is not the isotropic 2 mu + lambda (patch 7)."""
     diag = diag or strain
     if REF_SRC.exists() and (force or not PATCHED.exists()
                              or PATCHED.stat().st_mtime < Path(__file__).stat().st_mtime):
         write_patched_source()
     if not PATCHED.exists():
         raise FileNotFoundError("patched reference source missing (no reference checkout here)")
-    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d, dslip, uq2)
+    out = REF_DIR / binary_name(n, k, sigma, fp64, diag, setup_b, asf, cd2, strain, d, dslip, uq2, mu, lam, c11)
     if out.exists() and out.stat().st_mtime >= PATCHED.stat().st_mtime and not force:
         return out
     defs = [f"-DPFDD_N1={n[0]}", f"-DPFDD_N2={n[1]}", f"-DPFDD_N3={n[2]}", f"-DPFDD_K={k}",
@@ -263,6 +278,8 @@ def compile_ref(n=(32, 32, 32), k=20, sigma=0.0, fp64=True, diag=False, setup_b=
             f"-DPFDD_STRAIN_OUT={1 if strain else 0}",
             f"-DPFDD_D1={float(d[0])!r}", f"-DPFDD_D2={float(d[1])!r}", f"-DPFDD_D3={float(d[2])!r}",
             f"-DPFDD_DSLIP={float(dslip)!r}", f"-DPFDD_UQ2={float(uq2)!r}"]
+    if c11 is not None:  # a cubic material: MT 1 (isotropic) would reset C11 to 2 mu + lambda (F:4243-4244)
+        defs += [f"-DPFDD_C11={float(c11)!r}", "-DPFDD_MT=2"]
     if fp64:
         defs.append("-Dfloat=double")
     cmd = ["gcc", "-O2", "-w", "-DUSE_FOURN", *defs]

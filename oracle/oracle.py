@@ -132,7 +132,7 @@ def solve(spec, steps: int | None = None, eps_bdiv: float = float(np.sqrt(2.0)))
     K = spec.steps if steps is None else steps
     eps = fcc_eps(spec.ns, bdiv=eps_bdiv, dslip=np.full(12, spec.dslip))
     C44, C12 = spec.mu, spec.lam
-    C11 = 2.0 * C44 + C12
+    C11 = spec.C11
     B = bmatrix(spec.n, eps, C11, C12, C44, spec.d)
     sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
     tau_max = resolved_shear(eps, sig)

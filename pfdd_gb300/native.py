@@ -430,7 +430,7 @@ def solver_for(spec: workloads.SolveSpec, precision: str = "fp64", nrep: int = 1
     s = Solver(spec.n, spec.ns, precision, nrep, device)
     eps = fcc_eps(spec.ns, dslip=spec.dslip)
     C44, C12 = spec.mu, spec.lam
-    s.build_B(2.0 * C44 + C12, C12, C44, eps, spec.d)
+    s.build_B(spec.C11, C12, C44, eps, spec.d)
     s.set_params(spec.cd2, spec.asf, spec.dslip, spec.uq2)
     return s
 

@@ -92,7 +92,7 @@ class Server:
         tau_max = native.resolved_shear(eps, sig)
         xi, bc = workloads.initial_state(spec)
         C44, C12 = spec.mu, spec.lam
-        return self.submit_raw(spec.n, spec.ns, spec.steps, 2.0 * C44 + C12, C12, C44, eps, tau_max, xi, bc,
+        return self.submit_raw(spec.n, spec.ns, spec.steps, spec.C11, C12, C44, eps, tau_max, xi, bc,
                                cd2=spec.cd2, asf=spec.asf, dslip=spec.dslip, uq2=spec.uq2, d=spec.d,
                                converge=converge)
 

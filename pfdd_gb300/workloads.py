@@ -17,7 +17,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
-from typing import List, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -75,10 +75,17 @@ class SolveSpec:
     pin_frac: float = 0.0     # fraction of every field's points held fixed (xi_bc = 1)
     pin_seed: int = 0
     uq2: float = 1.0          # factor of the elastic force in the update (F:3488-3489)
+    c11: Optional[float] = None  # C11 of a cubic material; None: isotropic, 2 mu + lambda
 
     @property
     def lam(self) -> float:
         return 2.0 * self.mu * self.nu / (1.0 - 2.0 * self.nu)
+
+    @property
+    def C11(self) -> float:
+        """Elastic constants (C11, C12 = lambda, C44 = mu) as the reference's
+        material struct holds them."""
+        return 2.0 * self.mu + self.lam if self.c11 is None else float(self.c11)
 
     @property
     def npts(self) -> int:

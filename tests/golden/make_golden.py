@@ -64,6 +64,11 @@ def cases():
     yield "fcc12_32x16x8_uq2_k30", workloads.SolveSpec(
         n=(32, 16, 8), ns=12, steps=30, sigma_max=0.05,
         loops=workloads.random_loops((32, 16, 8), 3, 2.0, 4.0, 12, seed=51), noise_seed=51, uq2=0.6)
+    # a cubic material (C11 != 2 mu + lambda) with mu = 1.5
+    yield "fcc12_16x16x32_cubic_k30", workloads.SolveSpec(
+        n=(16, 16, 32), ns=12, steps=30, sigma_max=0.08,
+        loops=workloads.random_loops((16, 16, 32), 3, 2.0, 4.0, 12, seed=61), noise_seed=61,
+        mu=1.5, nu=0.3, c11=6.0)
 
 
 def spec_json(spec: workloads.SolveSpec) -> str:
@@ -74,7 +79,7 @@ def spec_json(spec: workloads.SolveSpec) -> str:
 def run_case(name: str, spec: workloads.SolveSpec, fp64: bool, krun: int | None = None):
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=fp64,
                               asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d,
-                              dslip=spec.dslip, uq2=spec.uq2)
+                              dslip=spec.dslip, uq2=spec.uq2, c11=spec.c11)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)
@@ -138,7 +143,7 @@ def make_oracle_long(name: str = "oracle_config1_128c_ns12_k1000", every: int = 
     spec = workloads.config1()
     eps = orc.fcc_eps(spec.ns, dslip=np.full(12, spec.dslip))
     C44, C12 = spec.mu, spec.lam
-    B = orc.bmatrix(spec.n, eps, 2.0 * C44 + C12, C12, C44, spec.d)
+    B = orc.bmatrix(spec.n, eps, spec.C11, C12, C44, spec.d)
     sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
     tau = orc.ramp_tau(orc.resolved_shear(eps, sig), spec.steps)
     xi, bc = workloads.initial_state(spec)
