@@ -1,6 +1,8 @@
 """The recipe that builds the patched reference (oracle/build_ref.py): a cached
 binary is reused only for the configuration it was built for, so every value
 the build takes from -D must show in the binary's name."""
+import pytest
+
 from oracle import build_ref
 
 BASE = dict(n=(16, 8, 32), k=30, sigma=0.05)
@@ -33,7 +35,6 @@ def test_patches_are_in_line_order_and_name_their_text():
 def test_patch_set_applies_to_the_reference_source(tmp_path):
     """Every patch finds its original text on its line (the recipe refuses a
     different revision of the reference rather than building something else)."""
-    import pytest
     if not build_ref.REF_SRC.exists():
         pytest.skip("no reference checkout here")
     out = build_ref.write_patched_source(dst=tmp_path / "patched.c")
