@@ -227,11 +227,17 @@ def strain_cases():
     c0 = workloads.config0()
     c0.steps = 2
     yield "strain_config0_32c_ns3", c0
+    # anisotropic grid spacing, slip-plane spacing 2, mu = 1.5, nu = 0.25
+    yield "strain_fcc12_16x8x16_aniso", workloads.SolveSpec(
+        n=(16, 8, 16), ns=12, steps=2, sigma_max=0.05,
+        loops=workloads.random_loops((16, 8, 16), 3, 2.0, 4.0, 12, seed=71), noise_seed=71,
+        mu=1.5, nu=0.25, dslip=2.0, d=(2.0, 1.0, 0.5))
 
 
 def make_strain(name: str, spec: workloads.SolveSpec):
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=True, strain=True,
-                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d,
+                              dslip=spec.dslip, uq2=spec.uq2, c11=spec.c11)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)

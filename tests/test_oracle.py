@@ -116,9 +116,9 @@ def test_pinned_points_do_not_move():
 def strain_inputs(spec):
     """Initial state, eigenstrains, constants and applied stress of a strain golden case."""
     xi, _ = workloads.initial_state(spec)
-    eps = oracle.fcc_eps(12)[:spec.ns]
+    eps = oracle.fcc_eps(12, dslip=np.full(12, spec.dslip))[:spec.ns]
     sig = np.zeros((3, 3)); sig[0, 2] = sig[2, 0] = spec.sigma_max
-    return xi, eps, 2 * spec.mu + spec.lam, spec.lam, spec.mu, sig
+    return xi, eps, spec.C11, spec.lam, spec.mu, sig
 
 
 @pytest.mark.parametrize("name", strain_golden_cases())
@@ -128,7 +128,7 @@ def test_oracle_strain_stress_matches_reference(name):
     averages against the reference's stress-strain.dat (printed with %e)."""
     spec, z = load_golden(name)
     xi, eps, C11, C12, C44, sig = strain_inputs(spec)
-    e, s, ae, asg = oracle.strain_stress(spec.n, xi, eps, C11, C12, C44, sig)
+    e, s, ae, asg = oracle.strain_stress(spec.n, xi, eps, C11, C12, C44, sig, spec.d)
     e, s = e.reshape(9, -1), s.reshape(9, -1)
     if "eps" in z:
         re, rs = z["eps"], z["sigma"]
