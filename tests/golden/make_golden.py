@@ -192,12 +192,18 @@ def diag_cases():
     yield "diag_fcc12_16x8x32_k12", workloads.SolveSpec(
         n=(16, 8, 32), ns=12, steps=12, sigma_max=0.06,
         loops=workloads.random_loops((16, 8, 32), 4, 2.0, 5.0, 12, seed=41), noise_seed=41)
+    # mu = 1.5, nu = 0.25, slip-plane spacing 2, Asf and CD2 off their defaults
+    yield "diag_fcc12_16x8x16_mu15_k10", workloads.SolveSpec(
+        n=(16, 8, 16), ns=12, steps=10, sigma_max=0.05,
+        loops=workloads.random_loops((16, 8, 16), 3, 2.0, 4.0, 12, seed=81), noise_seed=81,
+        mu=1.5, nu=0.25, dslip=2.0, asf=0.12, cd2=0.015)
 
 
 def make_diag(name: str, spec: workloads.SolveSpec):
     import re
     b = build_ref.compile_ref(n=spec.n, k=spec.steps, sigma=spec.sigma_max, fp64=True, diag=True,
-                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam)
+                              asf=spec.asf, cd2=spec.cd2, mu=spec.mu, lam=spec.lam, d=spec.d,
+                              dslip=spec.dslip, uq2=spec.uq2, c11=spec.c11)
     d = Path(tempfile.mkdtemp(prefix=f"golden_{name}_"))
     try:
         xi, bc = workloads.initial_state(spec)

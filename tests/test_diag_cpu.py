@@ -4,7 +4,7 @@ energy_in3 and energy_in4 and the outer lines, from the oracle's states."""
 import numpy as np
 import pytest
 
-from conftest import diag_golden_cases, load_golden
+from conftest import check_residual, diag_golden_cases, load_golden
 from oracle import diag, oracle
 from pfdd_gb300 import native, workloads
 
@@ -14,10 +14,10 @@ def test_restated_energies_match_reference(name):
     spec, z = load_golden(name)
     outer, inner, D = z["energy_outer"], z["energy_inner"], z["D"]
     C44, C12 = spec.mu, spec.lam
-    p = native.reference_diag_params(spec.n, spec.sigma_max, 2.0 * C44 + C12, C12, C44, D=D)
-    eps = oracle.fcc_eps(spec.ns)
+    p = native.reference_diag_params(spec.n, spec.sigma_max, spec.C11, C12, C44, D=D)
+    eps = oracle.fcc_eps(spec.ns, dslip=np.full(12, spec.dslip))
     xi, bc = workloads.initial_state(spec)
-    B = oracle.bmatrix(spec.n, eps, 2.0 * C44 + C12, C12, C44)
+    B = oracle.bmatrix(spec.n, eps, spec.C11, C12, C44, spec.d)
     tau = oracle.ramp_tau(oracle.resolved_shear(eps, np.array([[0, 0, spec.sigma_max], [0, 0, 0],
                                                                [spec.sigma_max, 0, 0]])), spec.steps)
     ns = spec.ns
@@ -27,18 +27,18 @@ def test_restated_energies_match_reference(name):
     # outer line of the initial state (before the inner loop): one call's energy_in4
     np.testing.assert_allclose(outer[0, 3:5], e0[2:4], rtol=1e-13)
     assert outer[0, 1] == 0.0 and outer[0, 2] == 0.0
-    # one-material runs: calculateD4int reads the second material out of range,
-    # D10 / D11 come out NaN and so do energy_Residual and the total
-    assert np.isnan(D[2]) and np.isnan(outer[0, 5]) and np.isnan(e0[4])
+    # energy_Residual and the total from the reference's D coefficients
+    check_residual(outer[0, 5:7], e0[4:6])
     for s in range(spec.steps):
         xi, _, _ = oracle.run(spec.n, B, xi, bc, np.full(ns, spec.cd2), np.full(ns, spec.asf),
-                              np.full(ns, spec.dslip), 1.0, tau[s:s + 1])
+                              np.full(ns, spec.dslip), spec.uq2, tau[s:s + 1])
         e = diag.energies(xi.real, eps, p)
         assert abs(inner[s, 3] - e[2]) <= 1e-12 * scale3, s
         # the reference adds one call's energy_in4 per call, from the outer
         # step's call on: s + 2 calls by inner step s
         np.testing.assert_allclose(inner[s, 4], (s + 2) * e[3], rtol=1e-12)
-        assert inner[s, 1] == 0.0 and inner[s, 2] == 0.0 and np.isnan(inner[s, 5]) and np.isnan(e[4])
+        assert inner[s, 1] == 0.0 and inner[s, 2] == 0.0
+        check_residual(inner[s, 5], e[4])
     # the outer line after the inner loop: the final state's energy_in3
     np.testing.assert_allclose(outer[-1, 3], diag.energies(xi.real, eps, p)[2], rtol=1e-12)
 

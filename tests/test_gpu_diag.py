@@ -6,7 +6,7 @@ and energy_in4, the final state's line; in both forms and in a batch."""
 import numpy as np
 import pytest
 
-from conftest import diag_golden_cases, load_golden
+from conftest import check_residual, diag_golden_cases, load_golden
 from oracle import diag, oracle
 from pfdd_gb300 import native, workloads
 
@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 def run(spec, z, precision, nrep=1):
     C44, C12 = spec.mu, spec.lam
-    p = native.reference_diag_params(spec.n, spec.sigma_max, 2.0 * C44 + C12, C12, C44, D=z["D"])
+    p = native.reference_diag_params(spec.n, spec.sigma_max, spec.C11, C12, C44, D=z["D"])
     s = native.solver_for(spec, precision, nrep=nrep)
     try:
         x0, b0 = workloads.initial_state(spec)
@@ -41,10 +41,11 @@ def test_diagnostics_match_reference(native_lib, name):
     e0, e, ef, launches = run(spec, z, "fp64")
     assert launches == 5 * spec.steps + 1 or launches >= 5 * spec.steps  # the gather runs every step
     np.testing.assert_allclose(e0[0, 2:4], outer[0, 3:5], rtol=1e-13)
-    assert e0[0, 0] == 0.0 and e0[0, 1] == 0.0 and np.isnan(e0[0, 4]) and np.isnan(e0[0, 5])
+    assert e0[0, 0] == 0.0 and e0[0, 1] == 0.0
+    check_residual(outer[0, 5:7], e0[0, 4:6])
     assert np.max(np.abs(e[:, 0, 2] - inner[:, 3])) <= 1e-12 * scale3
     np.testing.assert_allclose((np.arange(spec.steps) + 2) * e[:, 0, 3], inner[:, 4], rtol=1e-12)
-    assert np.all(np.isnan(e[:, 0, 4])) and np.all(np.isnan(inner[:, 5]))
+    check_residual(inner[:, 5], e[:, 0, 4])
     assert abs(ef[0, 2] - outer[-1, 3]) <= 1e-12 * scale3
     # the FP32-FFT form: within its tolerance; a batch of identical replicas: the same bits
     _, e32, _, _ = run(spec, z, "fp32")
