@@ -77,7 +77,14 @@ def test_argument_validation_before_any_device_call(native_lib):
     assert native_lib.pfdd_server_submit(None, None, C.byref(cnt)) == native.PFDD_EINVAL
     assert native_lib.pfdd_server_stats(None, None, None, None, None) == native.PFDD_EINVAL
     assert native_lib.pfdd_server_wait(None, 1, None, None, None) == native.PFDD_EINVAL
+    assert native_lib.pfdd_server_wait_run(None, 1, None, None, None, None) == native.PFDD_EINVAL
     native_lib.pfdd_server_destroy(None)
+    # convergence stop: no context
+    ran = (C.c_int * 1)()
+    assert native_lib.pfdd_converge_reset(None, 0.0) == native.PFDD_EINVAL
+    assert native_lib.pfdd_converge_reset_batched(None, None) == native.PFDD_EINVAL
+    assert native_lib.pfdd_step_converge(None, 1, None, None, None, ran) == native.PFDD_EINVAL
+    assert native_lib.pfdd_step_converge_batched(None, 1, None, None, None, ran) == native.PFDD_EINVAL
 
 
 def test_required_bytes_scale():
@@ -134,3 +141,23 @@ def test_reference_patch_recipe_applies():
     out = br.write_patched_source(dst=ROOT / "oracle" / "_ref" / "pfdd_ref_patched.c")
     text = out.read_text(encoding="latin-1")
     assert "#define NS1 12" in text and "if(0) {" in text and "PFDD_LOG_STEP" in text
+
+
+def test_every_context_call_rejects_a_null_handle(native_lib):
+    """Each entry point that takes a context or plan returns PFDD_EINVAL for a
+    null one before touching the device (its first check), with every other
+    argument null or zero."""
+    import ctypes as C
+    names = ["pfdd_set_B", "pfdd_get_B", "pfdd_build_B", "pfdd_set_params", "pfdd_set_state",
+             "pfdd_set_replica_state", "pfdd_set_tau_field", "pfdd_set_replica_active", "pfdd_step",
+             "pfdd_converge_reset", "pfdd_converge_reset_batched", "pfdd_step_converge",
+             "pfdd_step_converge_batched", "pfdd_get_plan", "pfdd_set_diagnostics", "pfdd_get_diagnostics",
+             "pfdd_state_diagnostics", "pfdd_get_state", "pfdd_get_replica_state", "pfdd_set_stream_priority",
+             "pfdd_set_kernel_timing", "pfdd_kernel_stat", "pfdd_fft_forward", "pfdd_fft_backward",
+             "pfdd_strain_stress"]
+    for name in names:
+        fn = getattr(native_lib, name)
+        assert fn.argtypes, name
+        args = [0.0 if t is C.c_double else 0 if t in (C.c_int, C.c_size_t, C.c_longlong) else None
+                for t in fn.argtypes]
+        assert fn(*args) == native.PFDD_EINVAL, name
