@@ -53,7 +53,7 @@ int main() {
   const int sizes[][3] = {{8, 8, 8}, {16, 16, 16}, {32, 32, 32}, {64, 64, 64}, {128, 128, 128}, {256, 256, 256},
                           {8, 16, 32}, {32, 2, 32}, {16, 8, 32}, {32, 16, 64}, {8, 16, 16}, {16, 8, 16}, {16, 16, 32},
                           {512, 8, 8}, {8, 8, 512}, {4, 4, 4}, {2, 64, 2}, {16, 1, 16}, {1, 16, 32}, {16, 16, 1},
-                          {2, 4, 8}, {512, 2, 2}, {2, 2, 512}, {1, 1, 1}};
+                          {2, 4, 8}, {512, 2, 2}, {2, 2, 512}, {1, 1, 1}, {32, 8, 16}, {16, 32, 8}, {32, 16, 8}};
   const size_t vb[3][2] = {{16, 8}, {8, 4}, {8, 0}};
   for (auto &sz : sizes)
     for (int ns : {1, 3, 12})
