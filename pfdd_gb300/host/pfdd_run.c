@@ -17,8 +17,15 @@
  * F:3732-3785) and the files hold the steps that ran.
  *
  * usage: pfdd_run N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C]
- *                 [--mu MU] [--lambda LAM] [--bdiv BD] [--fp32] [--device D]
+ *                 [--mu MU] [--lambda LAM] [--c11 C11] [--dslip DS] [--uq2 U]
+ *                 [--d D1 D2 D3] [--bdiv BD] [--fp32] [--device D]
  *                 [--strain] [--converge]
+ *
+ * MU, LAM: C44 and C12 (F:302-304); C11 defaults to the isotropic 2 MU + LAM
+ * (F:4243-4244), --c11 gives a cubic material (the reference's MT 2).  DS: the
+ * slip-plane spacing (dslip, F:4209), U: the update's force factor (uq2,
+ * F:4195), D1 D2 D3: the grid spacing (d1, d2, d3, F:4269-4271); all 1 by
+ * default, as the reference sets them.
  *
  * NSF (default NS) is the slip-system count of the files; systems NS..NSF-1
  * and the 9 virtual-strain fields must be zero and pinned (they contribute
@@ -76,19 +83,27 @@ static int write_fields(int n1, int n2, int n3, const double *e, const double *s
 int main(int argc, char **argv) {
   if (argc < 7) {
     fprintf(stderr, "usage: %s N1 N2 N3 NS K SIGMA [--nsfile NSF] [--asf A] [--cd2 C] [--mu MU] [--lambda LAM] "
-                    "[--bdiv BD] [--fp32] [--device D] [--strain] [--converge]\n", argv[0]);
+                    "[--c11 C11] [--dslip DS] [--uq2 U] [--d D1 D2 D3] [--bdiv BD] [--fp32] [--device D] [--strain] "
+                    "[--converge]\n", argv[0]);
     return 2;
   }
   int n1 = atoi(argv[1]), n2 = atoi(argv[2]), n3 = atoi(argv[3]), ns = atoi(argv[4]), K = atoi(argv[5]);
   double sigma_max = atof(argv[6]);
   int nsf = ns, prec = PFDD_FP64, dev = 0, strain = 0, conv = 0;
   double asf = 0.1, cd2 = 0.01, mu = 1.0, lam = 1.5, bdiv = sqrt(2.0);
+  double c11 = NAN, dsl = 1.0, uq2 = 1.0, dd[3] = {1.0, 1.0, 1.0};
   for (int i = 7; i < argc; ++i) {
     if (!strcmp(argv[i], "--nsfile") && i + 1 < argc) nsf = atoi(argv[++i]);
     else if (!strcmp(argv[i], "--asf") && i + 1 < argc) asf = atof(argv[++i]);
     else if (!strcmp(argv[i], "--cd2") && i + 1 < argc) cd2 = atof(argv[++i]);
     else if (!strcmp(argv[i], "--mu") && i + 1 < argc) mu = atof(argv[++i]);
     else if (!strcmp(argv[i], "--lambda") && i + 1 < argc) lam = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--c11") && i + 1 < argc) c11 = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--dslip") && i + 1 < argc) dsl = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--uq2") && i + 1 < argc) uq2 = atof(argv[++i]);
+    else if (!strcmp(argv[i], "--d") && i + 3 < argc) {
+      for (int q = 0; q < 3; ++q) dd[q] = atof(argv[++i]);
+    }
     else if (!strcmp(argv[i], "--bdiv") && i + 1 < argc) bdiv = atof(argv[++i]);
     else if (!strcmp(argv[i], "--fp32")) prec = PFDD_FFT_FP32;
     else if (!strcmp(argv[i], "--device") && i + 1 < argc) dev = atoi(argv[++i]);
@@ -97,6 +112,11 @@ int main(int argc, char **argv) {
     else { fprintf(stderr, "unknown option %s\n", argv[i]); return 2; }
   }
   if (ns < 1 || ns > 12 || nsf < ns || K < 1) { fprintf(stderr, "bad NS/K\n"); return 2; }
+  if (!(dsl > 0) || !(dd[0] > 0) || !(dd[1] > 0) || !(dd[2] > 0) || !isfinite(uq2) || !isfinite(dsl) ||
+      !isfinite(dd[0]) || !isfinite(dd[1]) || !isfinite(dd[2])) {
+    fprintf(stderr, "bad spacing or force factor\n");
+    return 2;
+  }
   const long N = (long)n1 * n2 * n3;
   const int nsv = nsf + 9;
   const size_t cnt = (size_t)2 * nsv * N;
@@ -115,9 +135,10 @@ int main(int argc, char **argv) {
     }
 
   /* setup (F:4253-4330) */
-  double C44 = mu, C12 = lam, C11 = 2. * C44 + C12; /* isotropic: C11 = 2 C44 + C12, F:4243-4245 */
+  /* isotropic: C11 = 2 C44 + C12 (F:4243-4245); a cubic C11 with --c11 */
+  double C44 = mu, C12 = lam, C11 = isnan(c11) ? 2. * C44 + C12 : c11;
   double xn[12][3], xb[12][3], th[3][3], dslip[12], eps[12][3][3], tau_max[12];
-  for (int s = 0; s < 12; ++s) dslip[s] = 1.0;
+  for (int s = 0; s < 12; ++s) dslip[s] = dsl;
   pfdd_setfcc(xn, xb, bdiv);
   pfdd_setorient(th);
   pfdd_seteps(12, (const double(*)[3])xn, (const double(*)[3])xb, dslip, (const double(*)[3])th, eps);
@@ -132,8 +153,8 @@ int main(int argc, char **argv) {
   int st;
   double t0 = wtime();
   if ((st = pfdd_create(&c, n1, n2, n3, ns, prec, dev)) != PFDD_OK) return die("create", c, st);
-  if ((st = pfdd_build_B(c, C11, C12, C44, &eps[0][0][0], 1.0, 1.0, 1.0)) != PFDD_OK) return die("build_B", c, st);
-  if ((st = pfdd_set_params(c, cdv, asfv, dslip, 1.0)) != PFDD_OK) return die("set_params", c, st);
+  if ((st = pfdd_build_B(c, C11, C12, C44, &eps[0][0][0], dd[0], dd[1], dd[2])) != PFDD_OK) return die("build_B", c, st);
+  if ((st = pfdd_set_params(c, cdv, asfv, dslip, uq2)) != PFDD_OK) return die("set_params", c, st);
   if ((st = pfdd_set_state(c, xi, bc)) != PFDD_OK) return die("set_state", c, st);
   double *gamma = malloc(sizeof(double) * K), *gamma_a = malloc(sizeof(double) * (size_t)K * ns);
   double ave0[2][9], ave1[2][9];

@@ -59,3 +59,14 @@ def test_bad_arguments_are_rejected(native_lib, tmp_path):
     assert r.returncode == 2 and "unknown option" in r.stderr
     r = subprocess.run([str(build.RUNNER), "8", "8"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_bad_spacing_and_force_factor_are_rejected(native_lib, tmp_path):
+    _write(tmp_path)
+    for extra in (["--dslip", "0"], ["--d", "1", "0", "1"], ["--d", "1", "-2", "1"], ["--uq2", "nan"],
+                  ["--d", "1", "inf", "1"]):
+        r = _run(tmp_path, *extra)
+        assert r.returncode == 2 and "bad spacing or force factor" in r.stderr, extra
+        assert not (tmp_path / "phasefield.dat").exists()
+    r = _run(tmp_path, "--d", "1", "1")  # three values or none
+    assert r.returncode == 2 and "unknown option" in r.stderr
